@@ -1,0 +1,243 @@
+/* lpm_gb300.h -- C ABI of the GB300 (sm_103a) direct-summation Biot-Savart
+ * library.
+ *
+ * This is the drop-in boundary for LPM's direct-sum hot path.  Each entry point
+ * replaces one Kokkos launch of the reference,
+ *
+ *     Kokkos::parallel_for(label, TeamPolicy<>(n_targets, AUTO()), Functor(...));
+ *
+ * with the same arguments in plain pointers and sizes, or one stepper method
+ * (BVERK4::advance_timestep, Incompressible2DRK2::advance_timestep_impl).
+ * Reference file:line citations are relative to the pbosler/lpm source tree.
+ *
+ * Conventions
+ *  - All array pointers are DEVICE pointers owned by the caller; nothing is
+ *    retained after a call returns (steppers keep only their own workspace).
+ *  - Coordinates and vectors are passed as strided views (lpm_view): element
+ *    (i, c) lives at p[i * stride_i + c * stride_c].  Kokkos LayoutRight (AoS)
+ *    is stride_i = ndim, stride_c = 1; LayoutLeft (SoA, the Kokkos-CUDA default
+ *    for View<Real*[3]>) is stride_i = 1, stride_c = nmax.
+ *  - Masks are one byte per face slot, nonzero = divided face (excluded as a
+ *    source), as View<bool*> in the reference.
+ *  - Real = double, Index = 64-bit here (the reference uses int).
+ *  - Calls are asynchronous and ordered on the context's CUDA stream, except
+ *    where a host result is returned (invariants, error norms, timing).
+ *  - Every call returns LPM_OK (0) or a negative code; lpm_last_error() gives
+ *    a message (thread-local).  The C++ facade (lpm_gb300.hpp) turns nonzero
+ *    codes into std::runtime_error, as LPM_REQUIRE does
+ *    (src/lpm_assert.hpp:22-30).
+ *  - One context per host thread; a context is not thread-safe.
+ */
+#ifndef LPM_GB300_H
+#define LPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define LPM_OK 0
+#define LPM_ERR_ARG (-1)     /* invalid argument (null pointer, size, stride) */
+#define LPM_ERR_CUDA (-2)    /* CUDA runtime error */
+#define LPM_ERR_TIMEOUT (-3) /* a bounded device-side wait gave up */
+#define LPM_ERR_ALLOC (-4)   /* device allocation failed */
+#define LPM_ERR_STATE (-5)   /* object used in the wrong state */
+
+/* ---- arithmetic of the pairwise sum ------------------------------------ */
+/* LPM_FP64: every pair term in FP64 in the reference's evaluation order.
+ * LPM_FP32C: FP32 pair kernel (denominator rebuilt as |x-y|^2/2 + eps^2),
+ *            per-tile Kahan/TwoSum-compensated sums, FP64 epilogue. */
+#define LPM_FP64 64
+#define LPM_FP32C 32
+
+/* geometry */
+#define LPM_PLANE 2
+#define LPM_SPHERE 3
+
+typedef struct {
+  double* p;
+  int64_t stride_i;
+  int64_t stride_c;
+} lpm_view;
+
+typedef struct lpm_context lpm_context;
+
+/* ---- context ----------------------------------------------------------- */
+/* Binds a CUDA device.  The context owns cached device scratch (packed source
+ * tiles, per-chunk partial sums) that grows on demand. */
+int lpm_context_create(lpm_context** ctx, int device);
+int lpm_context_destroy(lpm_context* ctx);
+/* cudaStream_t passed as void*; 0 = the legacy default stream. */
+int lpm_context_set_stream(lpm_context* ctx, void* cuda_stream);
+/* LPM_FP64 (default) or LPM_FP32C for the functor entry points below. */
+int lpm_context_set_precision(lpm_context* ctx, int precision);
+/* Waits for the context's stream, then reports LPM_ERR_TIMEOUT if a bounded
+ * device-side wait gave up since the last check (and clears the flag). */
+int lpm_context_synchronize(lpm_context* ctx);
+/* Number of CUDA kernels this context has launched so far. */
+int64_t lpm_context_kernel_launches(const lpm_context* ctx);
+/* Thread-local message for the last failing call on this thread. */
+const char* lpm_last_error(void);
+/* 1 if the library was built for the GPU in this process, 0 otherwise. */
+int lpm_device_count(void);
+
+/* ---- BVE direct sums on the sphere (src/lpm_bve_sphere_kernels.hpp) ----- */
+/* BVEVertexSolve (:90-132): psi (nullable) and u (u.p nullable) at nverts
+ * vertex targets from nfaces face slots (vorticity zeta, area, mask). */
+int lpm_bve_vertex_solve(lpm_context* ctx, double* psi, lpm_view u,
+                         lpm_view vx, int64_t nverts, lpm_view fx,
+                         const double* zeta, const double* area,
+                         const uint8_t* mask, int64_t nfaces);
+/* BVEVertexStreamFn (:141-170). */
+int lpm_bve_vertex_stream_fn(lpm_context* ctx, double* psi, lpm_view vx,
+                             int64_t nverts, lpm_view fx, const double* zeta,
+                             const double* area, const uint8_t* mask,
+                             int64_t nfaces);
+/* BVEVertexVelocity (:179-211). */
+int lpm_bve_vertex_velocity(lpm_context* ctx, lpm_view u, lpm_view vx,
+                            int64_t nverts, lpm_view fx, const double* zeta,
+                            const double* area, const uint8_t* mask,
+                            int64_t nfaces);
+/* BVEFaceSolve (:284-320): collocated face targets, i == j skipped. */
+int lpm_bve_face_solve(lpm_context* ctx, double* psi, lpm_view u, lpm_view fx,
+                       const double* zeta, const double* area,
+                       const uint8_t* mask, int64_t nfaces);
+/* BVEFaceStreamFn (:329-356). */
+int lpm_bve_face_stream_fn(lpm_context* ctx, double* psi, lpm_view fx,
+                           const double* zeta, const double* area,
+                           const uint8_t* mask, int64_t nfaces);
+/* BVEFaceVelocity (:365-394). */
+int lpm_bve_face_velocity(lpm_context* ctx, lpm_view u, lpm_view fx,
+                          const double* zeta, const double* area,
+                          const uint8_t* mask, int64_t nfaces);
+/* BVEVorticityTendency (:399-413): dzeta(i) = -2*Omega*u(i,2)*dt. */
+int lpm_bve_vorticity_tendency(lpm_context* ctx, double* dzeta, lpm_view u,
+                               int64_t n, double dt, double Omega);
+
+/* ---- incompressible2d (src/lpm_incompressible2d_kernels.hpp) ----------- */
+/* Incompressible2DPassiveSums<Geo> (:144-193); ndim = LPM_SPHERE or
+ * LPM_PLANE; u.p and psi nullable. */
+int lpm_ic2d_passive_sums(lpm_context* ctx, int ndim, lpm_view u, double* psi,
+                          lpm_view x, int64_t n_passive, lpm_view y,
+                          const double* zeta, const double* area,
+                          const uint8_t* mask, double eps, int64_t n_active);
+/* Incompressible2DActiveSums<Geo> (:201-246).  As in the reference the
+ * i == j term is skipped only when eps is zero (:235); self_rule = 1 skips it
+ * always (the rule of the BVE face functors). */
+int lpm_ic2d_active_sums(lpm_context* ctx, int ndim, lpm_view u, double* psi,
+                         lpm_view xy, const double* zeta, const double* area,
+                         const uint8_t* mask, double eps, int64_t n_active,
+                         int self_rule);
+/* Incompressible2DTendencies<Geo> (:257-278): dzeta = -dfdt(u), with
+ * CoriolisSphere(Omega) or CoriolisBetaPlane(f0, beta) (src/lpm_coriolis.hpp
+ * :97-195); cor = Omega (sphere) or beta (plane). */
+int lpm_ic2d_tendencies(lpm_context* ctx, int ndim, double* dzeta, lpm_view u,
+                        int64_t n, double cor);
+/* Incompressible2D::total_vorticity/total_enstrophy/total_kinetic_energy
+ * (src/lpm_incompressible2d_impl.hpp:91-137), FP64, deterministic order.
+ * out[0] = sum zeta*A, out[1] = 0.5 sum zeta^2 A, out[2] = 0.5 sum |u|^2 A
+ * over unmasked faces.  Synchronous. */
+int lpm_ic2d_invariants(lpm_context* ctx, int ndim, int64_t nfaces,
+                        const double* zeta, lpm_view vel, const double* area,
+                        const uint8_t* mask, double out[3]);
+
+/* ---- ErrNorms (src/lpm_error.hpp:81-91) -------------------------------- */
+/* Relative l1, l2 (weighted by wt; wt may be null = 1) and linf
+ * (max|err|/max|exact|) of vector magnitudes (ndim > 1) or values (ndim 1);
+ * mask (nullable) excludes entries.  Synchronous. */
+int lpm_err_norms(lpm_context* ctx, int ndim, int64_t n, lpm_view appx,
+                  lpm_view exact, const double* wt, const uint8_t* mask,
+                  double out[3]);
+
+/* ---- steppers ---------------------------------------------------------- */
+/* Step options (bit flags). */
+#define LPM_STEP_FIX_FACEVORT3 1u /* BVE: use stage-3 face vorticity in the
+                                     final update; the reference passes
+                                     facevort4 twice
+                                     (src/lpm_bve_rk4_impl.hpp:155-157) */
+#define LPM_STEP_REPROJECT 2u     /* renormalise positions to the unit sphere
+                                     after each step (the reference does not) */
+#define LPM_STEP_SKIP_MASKED_TARGETS 4u /* do not evaluate, nor move, divided
+                                     (masked) face slots; the reference
+                                     evaluates them although nothing reads
+                                     their values */
+#define LPM_STEP_SKIP_SELF_ALWAYS 8u /* ic2d: skip i == j also for eps > 0 */
+#define LPM_STEP_NO_GRAPH 16u     /* launch stages directly instead of
+                                     replaying a captured CUDA graph */
+
+typedef struct lpm_bve_rk4 lpm_bve_rk4;
+/* BVERK4(dt, sphere) + BVERK4::init (src/lpm_bve_rk4.hpp:10-77,
+ * src/lpm_bve_rk4.cpp:5-39): allocates the stage workspace for nverts
+ * vertices and nfaces face slots.  precision: LPM_FP64 or LPM_FP32C. eps is
+ * the kernel smoothing (0 = the reference BVE functors). */
+int lpm_bve_rk4_create(lpm_context* ctx, lpm_bve_rk4** out, int64_t nverts,
+                       int64_t nfaces, double dt, double Omega, double eps,
+                       int precision, uint32_t flags);
+int lpm_bve_rk4_destroy(lpm_bve_rk4* st);
+/* BVERK4::advance_timestep (src/lpm_bve_rk4_impl.hpp:55-167): advances
+ * positions and relative vorticity of vertices and faces by one RK4 step and
+ * leaves the velocities of the new state in vvel/fvel (which must hold the
+ * velocities of the current state on entry, as after
+ * BVESphere::init_velocity).  farea/fmask must not change between calls. */
+int lpm_bve_rk4_advance_timestep(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
+                                 lpm_view vvel, lpm_view fx, double* fzeta,
+                                 lpm_view fvel, const double* farea,
+                                 const uint8_t* fmask);
+
+typedef struct lpm_ic2d_rk2 lpm_ic2d_rk2;
+/* Incompressible2DRK2(dt, ic2d) (src/lpm_incompressible2d_rk2_impl.hpp:15-43).
+ * ndim = LPM_SPHERE or LPM_PLANE; cor = Coriolis Omega or beta. */
+int lpm_ic2d_rk2_create(lpm_context* ctx, lpm_ic2d_rk2** out, int ndim,
+                        int64_t nverts, int64_t nfaces, double dt, double eps,
+                        double cor, int precision, uint32_t flags);
+int lpm_ic2d_rk2_destroy(lpm_ic2d_rk2* st);
+/* Incompressible2DRK2::advance_timestep_impl (:74-172).  vvel/fvel/vpsi/fpsi
+ * hold the sums of the current state on entry (as after
+ * Incompressible2D::init_direct_sums) and of the new state on exit. */
+int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
+                                  double* vzeta, lpm_view vvel, double* vpsi,
+                                  lpm_view fx, double* fzeta, lpm_view fvel,
+                                  double* fpsi, const double* farea,
+                                  const uint8_t* fmask);
+
+/* ---- host-side inputs: meshes and initial conditions -------------------- */
+/* Mesh kinds (restatements of the reference seeds' tree_init,
+ * src/mesh/lpm_polymesh2d_impl.hpp:26-42, with the triangle and quad dividers
+ * of src/mesh/lpm_faces_impl.hpp:285-575). */
+#define LPM_MESH_ICOS_TRI 1     /* IcosTriSphereSeed */
+#define LPM_MESH_CUBED_SPHERE 2 /* CubedSphereSeed */
+#define LPM_MESH_QUAD_RECT 3    /* QuadRectSeed, [-radius, radius]^2 */
+/* Vertex count and face-slot count (all tree levels) for a uniform mesh. */
+int lpm_mesh_sizes(int kind, int level, int64_t* nverts, int64_t* nfaces);
+/* Fills HOST arrays: vx (nverts x ndim, AoS), fx (nfaces x ndim, AoS),
+ * farea (nfaces), fmask (nfaces; 1 = divided parent slot, area 0).  Face
+ * slots are ordered like the reference's tree (seed faces, then four children
+ * per divided face, level by level). */
+int lpm_mesh_build(int kind, int level, double radius, double* vx, double* fx,
+                   double* farea, uint8_t* fmask);
+
+/* Initial vorticity kinds (src/lpm_vorticity_gallery.hpp). */
+#define LPM_IC_SOLID_BODY 1      /* SolidBodyRotation: 2*OMEGA*z, OMEGA=2pi */
+#define LPM_IC_GAUSSIAN_SPHERE 2 /* params: strength, b, lon, lat, gauss_const,
+                                    background_Omega (adds 2*Omega*z) */
+#define LPM_IC_RH54 3            /* RossbyHaurwitz54: params u0, amplitude */
+#define LPM_IC_DIPOLE_PAIR 4     /* CollidingDipolePairPlane: strA, rA, xA, yA,
+                                    strB, rB, xB, yB */
+#define LPM_IC_MULTI_GAUSSIAN 5  /* sum of k Gaussians: params k, then per
+                                    vortex (strength, b, lon, lat) */
+/* Evaluates relative vorticity at n HOST points x (n x ndim, AoS). */
+int lpm_ic_eval(int kind, const double* params, int nparams, int ndim,
+                int64_t n, const double* x, double* zeta);
+
+/* ---- instrumentation ----------------------------------------------------- */
+/* Measured FP32 / FP64 FMA peak of this GPU (TFLOP/s) from a short
+ * register-only microbenchmark; synchronous. */
+int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LPM_GB300_H */

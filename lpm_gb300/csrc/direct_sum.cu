@@ -1,0 +1,686 @@
+// direct_sum.cu -- packing, N-body launch planning, combine epilogues and the
+// small O(N) device utilities behind the functor entry points.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lpm_host.hpp"
+#include "nbody.cuh"
+
+namespace lpm {
+
+namespace {
+
+constexpr int SCAN_BLOCK = 1024;
+
+__global__ void k_count_unmasked(const uint8_t* mask, int64_t n, int* bcount) {
+  __shared__ int warp_counts[SCAN_BLOCK / 32];
+  const int64_t i = (int64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x;
+  const int keep = (i < n && !mask[i]) ? 1 : 0;
+  const unsigned b = __ballot_sync(0xffffffffu, keep);
+  if ((threadIdx.x & 31) == 0) warp_counts[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < SCAN_BLOCK / 32; ++w) s += warp_counts[w];
+    bcount[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of nb block counts by one block; total in out[nb].
+__global__ void k_scan_counts(const int* bcount, int nb, int* boff) {
+  __shared__ int carry;
+  __shared__ int wsum[SCAN_BLOCK / 32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += SCAN_BLOCK) {
+    const int i = base + threadIdx.x;
+    const int v = i < nb ? bcount[i] : 0;
+    int x = v;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int w = wsum[threadIdx.x];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[threadIdx.x] = w;
+    }
+    __syncthreads();
+    const int wprefix = (threadIdx.x >= 32) ? wsum[(threadIdx.x >> 5) - 1] : 0;
+    const int incl = carry + wprefix + x;
+    if (i < nb) boff[i] = incl - v;
+    __syncthreads();
+    if (threadIdx.x == SCAN_BLOCK - 1) carry = incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) boff[nb] = carry;
+}
+
+__global__ void k_scatter_map(const uint8_t* mask, int64_t n, const int* boff,
+                              int* slot2src, int* src2slot) {
+  __shared__ int wbase[SCAN_BLOCK / 32];
+  const int64_t i = (int64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x;
+  const int keep = (i < n && !mask[i]) ? 1 : 0;
+  const unsigned b = __ballot_sync(0xffffffffu, keep);
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) wbase[threadIdx.x >> 5] = __popc(b);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < SCAN_BLOCK / 32; ++w) {
+      const int c = wbase[w];
+      wbase[w] = s;
+      s += c;
+    }
+  }
+  __syncthreads();
+  if (i < n) {
+    if (keep) {
+      const int k = boff[blockIdx.x] + wbase[threadIdx.x >> 5] +
+                    __popc(b & ((1u << lane) - 1u));
+      slot2src[i] = k;
+      src2slot[k] = int(i);
+    } else {
+      slot2src[i] = -1;
+    }
+  }
+}
+
+// Packed sources.  FP32: (x, y, z, zeta*area); FP64: (x, y, z, g) with
+// g = (-zeta)*area for the BVE form, zeta*area otherwise.
+template <bool F32>
+__global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
+                           View x, int ndim, const double* zeta,
+                           const double* area, int form, void* out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npad) return;
+  double p0 = 0, p1 = 0, p2 = 0, g = 0;
+  if (k < nsrc) {
+    const int64_t s = src2slot[k];
+    p0 = x(s, 0);
+    p1 = x(s, 1);
+    if (ndim == 3) p2 = x(s, 2);
+    g = (form == FORM_BVE && !F32) ? (-zeta[s]) * area[s] : zeta[s] * area[s];
+  }
+  if (F32) {
+    reinterpret_cast<float4*>(out)[k] = make_float4(
+        __double2float_rn(p0), __double2float_rn(p1), __double2float_rn(p2),
+        __double2float_rn(g));
+  } else {
+    reinterpret_cast<double4*>(out)[k] = make_double4(p0, p1, p2, g);
+  }
+}
+
+// Packed targets of one segment at offset off.  FP32: w = g of the skipped
+// self source (for the psi self-term correction), else 0.  FP64: tself.
+template <bool F32>
+__global__ void k_pack_tgt(int64_t off, int64_t n, View x, int ndim,
+                           const int* slot2src, bool skip_self,
+                           const double* zeta, const double* area, void* out,
+                           int* tself) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p0 = x(i, 0), p1 = x(i, 1), p2 = ndim == 3 ? x(i, 2) : 0.0;
+  int self = -1;
+  if (skip_self && slot2src) self = slot2src[i];
+  if (F32) {
+    float gs = 0.f;
+    if (self >= 0) gs = __double2float_rn(zeta[i] * area[i]);
+    reinterpret_cast<float4*>(out)[off + i] =
+        make_float4(__double2float_rn(p0), __double2float_rn(p1),
+                    __double2float_rn(p2), gs);
+  } else {
+    reinterpret_cast<double4*>(out)[off + i] = make_double4(p0, p1, p2, 0.0);
+    tself[off + i] = self;
+  }
+}
+
+__global__ void k_fill_pad_tgt(int64_t from, int64_t to, bool f32, void* out,
+                               int* tself) {
+  const int64_t i = from + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= to) return;
+  if (f32) {
+    reinterpret_cast<float4*>(out)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  } else {
+    reinterpret_cast<double4*>(out)[i] = make_double4(0, 0, 0, 0);
+    tself[i] = -1;
+  }
+}
+
+// Deterministic sum of the packed FP32 source strengths (two passes).
+__global__ void k_sum_g_partial(const float4* src, int64_t n, double* part) {
+  __shared__ double sh[256];
+  double s = 0;
+  for (int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * 256)
+    s += (double)src[k].w;
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void k_sum_final(const double* part, int n, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += part[i];
+    *out = s;
+  }
+}
+
+// Combine the chunk partials of one segment and write its outputs.
+template <bool F32, int NDIM, bool WU, bool WP>
+__global__ void k_combine(const double* __restrict__ part, int nchunks,
+                          int64_t ntgt_pad, int64_t off, int64_t n, View x,
+                          View u, double* psi, const float4* tgt32,
+                          const double* sg, float c0) {
+  constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t t = off + i;
+  double a[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) a[k] = 0.0;
+  for (int c = 0; c < nchunks; ++c) {
+    const double* p = part + (int64_t)c * NC * ntgt_pad + t;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) a[k] += p[k * ntgt_pad];
+  }
+  if (!F32) {
+    if (WU)
+#pragma unroll
+      for (int k = 0; k < NDIM; ++k) u(i, k) = a[k];
+    if (WP) psi[i] = a[NC - 1];
+    return;
+  }
+  constexpr double INV2PI = 1.0 / (2.0 * kPI);
+  constexpr double LN2_4PI = 0.69314718055994530942 / (4.0 * kPI);
+  if (WU) {
+    if (NDIM == 3) {
+      const double x0 = x(i, 0), x1 = x(i, 1), x2 = x(i, 2);
+      u(i, 0) = -INV2PI * (a[1] * x2 - a[2] * x1);
+      u(i, 1) = -INV2PI * (a[2] * x0 - a[0] * x2);
+      u(i, 2) = -INV2PI * (a[0] * x1 - a[1] * x0);
+    } else {
+      u(i, 0) = -INV2PI * a[1];
+      u(i, 1) = INV2PI * a[0];
+    }
+  }
+  if (WP) {
+    const float gs = tgt32[t].w;
+    double L = a[NC - 1] - (double)gs * (double)lg2_approx(c0);
+    if (NDIM == 3) L -= (*sg - (double)gs);
+    psi[i] = -LN2_4PI * L;
+  }
+}
+
+template <bool F32, int NDIM, bool WU, bool WP>
+void launch_combine(lpm_context& ctx, const NbodyPlan& p, const double* part,
+                    int64_t off, const TgtSeg& seg, const float4* tgt32,
+                    const double* sg, float c0) {
+  const int th = 256;
+  const int64_t nb = (seg.n + th - 1) / th;
+  k_combine<F32, NDIM, WU, WP><<<nb, th, 0, ctx.stream>>>(
+      part, p.nchunks, p.ntgt_pad, off, seg.n, seg.x, seg.u, seg.psi, tgt32,
+      sg, c0);
+  ctx.launches++;
+}
+
+template <bool F32, int NDIM>
+void combine_dispatch(lpm_context& ctx, const NbodyPlan& p, const double* part,
+                      int64_t off, const TgtSeg& seg, const float4* tgt32,
+                      const double* sg, float c0) {
+  if (p.wu && p.wp)
+    launch_combine<F32, NDIM, true, true>(ctx, p, part, off, seg, tgt32, sg, c0);
+  else if (p.wu)
+    launch_combine<F32, NDIM, true, false>(ctx, p, part, off, seg, tgt32, sg, c0);
+  else
+    launch_combine<F32, NDIM, false, true>(ctx, p, part, off, seg, tgt32, sg, c0);
+}
+
+template <int NDIM, bool WU, bool WP>
+void launch_f32(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                const void* src, double* part, float c0) {
+  dim3 grid(unsigned(p.ntgt_pad / (F32_NT * F32_R)), unsigned(p.nchunks));
+  nbody_f32<NDIM, WU, WP, F32_R, F32_NT, F32_TILE><<<grid, F32_NT, 0, ctx.stream>>>(
+      static_cast<const float4*>(tgt), static_cast<const float4*>(src),
+      p.ntgt_pad, p.nsrc_pad, p.chunk_len, c0, part, ctx.d_err);
+  ctx.launches++;
+}
+
+template <int FORM, bool WU, bool WP>
+void launch_f64(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                const int* tself, const void* src, double* part, double eps2) {
+  dim3 grid(unsigned(p.ntgt_pad / (F64_NT * F64_R)), unsigned(p.nchunks));
+  nbody_f64<FORM, WU, WP, F64_R, F64_NT, F64_TILE><<<grid, F64_NT, 0, ctx.stream>>>(
+      static_cast<const double4*>(tgt), tself, static_cast<const double4*>(src),
+      p.ntgt_pad, p.nsrc_pad, p.chunk_len, eps2, part, ctx.d_err);
+  ctx.launches++;
+}
+
+template <int FORM>
+void f64_want(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+              const int* tself, const void* src, double* part, double eps2) {
+  if (p.wu && p.wp)
+    launch_f64<FORM, true, true>(ctx, p, tgt, tself, src, part, eps2);
+  else if (p.wu)
+    launch_f64<FORM, true, false>(ctx, p, tgt, tself, src, part, eps2);
+  else
+    launch_f64<FORM, false, true>(ctx, p, tgt, tself, src, part, eps2);
+}
+
+template <int NDIM>
+void f32_want(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+              const void* src, double* part, float c0) {
+  if (p.wu && p.wp)
+    launch_f32<NDIM, true, true>(ctx, p, tgt, src, part, c0);
+  else if (p.wu)
+    launch_f32<NDIM, true, false>(ctx, p, tgt, src, part, c0);
+  else
+    launch_f32<NDIM, false, true>(ctx, p, tgt, src, part, c0);
+}
+
+int occupancy(int precision) {
+  static int occ32 = 0, occ64 = 0;
+  int& o = precision == LPM_FP32C ? occ32 : occ64;
+  if (o == 0) {
+    int v = 0;
+    if (precision == LPM_FP32C)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &v, nbody_f32<3, true, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &v, nbody_f64<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
+    o = v > 0 ? v : 1;
+  }
+  return o;
+}
+
+}  // namespace
+
+float f32_c0(int ndim, double eps) {
+  const double e2 = eps * eps;
+  return float((ndim == 3 ? 2.0 * e2 : e2) + 1e-30);
+}
+
+int64_t compact_sources(lpm_context& ctx, const uint8_t* mask, int64_t nslots,
+                        int* slot2src, int* src2slot) {
+  if (nslots == 0) return 0;
+  const int nb = int((nslots + SCAN_BLOCK - 1) / SCAN_BLOCK);
+  int* tmp = static_cast<int*>(ctx.arena.take(sizeof(int) * (2 * size_t(nb) + 1)));
+  int* bcount = tmp;
+  int* boff = tmp + nb;
+  k_count_unmasked<<<nb, SCAN_BLOCK, 0, ctx.stream>>>(mask, nslots, bcount);
+  k_scan_counts<<<1, SCAN_BLOCK, 0, ctx.stream>>>(bcount, nb, boff);
+  k_scatter_map<<<nb, SCAN_BLOCK, 0, ctx.stream>>>(mask, nslots, boff, slot2src,
+                                                   src2slot);
+  ctx.launches += 3;
+  LPM_CUDA(cudaGetLastError());
+  int total = 0;
+  LPM_CUDA(cudaMemcpyAsync(&total, boff + nb, sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx.stream));
+  LPM_CUDA(cudaStreamSynchronize(ctx.stream));
+  return total;
+}
+
+NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
+                     bool wu, bool wp, int64_t ntgt, int64_t nsrc) {
+  NbodyPlan p{};
+  p.precision = precision;
+  p.ndim = ndim;
+  p.form = form;
+  p.wu = wu;
+  p.wp = wp;
+  p.ncomp = (wu ? ndim : 0) + (wp ? 1 : 0);
+  const bool f32 = precision == LPM_FP32C;
+  const int tb = f32 ? F32_NT * F32_R : F64_NT * F64_R;
+  const int tile = f32 ? F32_TILE : F64_TILE;
+  p.ntgt = ntgt;
+  p.ntgt_pad = std::max<int64_t>(tb, (ntgt + tb - 1) / tb * tb);
+  p.nsrc = nsrc;
+  p.nsrc_pad = std::max<int64_t>(tile, (nsrc + tile - 1) / tile * tile);
+  const int64_t ntb = p.ntgt_pad / tb;
+  const int64_t ntiles = p.nsrc_pad / tile;
+  // Aim for ~16 waves of CTAs so the tail of the last wave stays small.
+  const int64_t slots = int64_t(std::max(ctx.num_sms, 1)) * occupancy(precision);
+  int64_t nch = (16 * slots + ntb - 1) / ntb;
+  nch = std::max<int64_t>(1, std::min<int64_t>(nch, ntiles));
+  const int64_t tiles_per_chunk = (ntiles + nch - 1) / nch;
+  p.chunk_len = int(tiles_per_chunk * tile);
+  p.nchunks = int((ntiles + tiles_per_chunk - 1) / tiles_per_chunk);
+  return p;
+}
+
+void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                  const int* tself, const void* src, double* part,
+                  double eps) {
+  if (p.precision == LPM_FP32C) {
+    const float c0 = f32_c0(p.ndim, eps);
+    if (p.ndim == 3)
+      f32_want<3>(ctx, p, tgt, src, part, c0);
+    else
+      f32_want<2>(ctx, p, tgt, src, part, c0);
+  } else {
+    const double eps2 = eps * eps;
+    if (p.form == FORM_BVE)
+      f64_want<0>(ctx, p, tgt, tself, src, part, eps2);
+    else if (p.form == FORM_SPHERE)
+      f64_want<1>(ctx, p, tgt, tself, src, part, eps2);
+    else
+      f64_want<2>(ctx, p, tgt, tself, src, part, eps2);
+  }
+  LPM_CUDA(cudaGetLastError());
+}
+
+void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
+                const TgtSeg* segs, int nseg) {
+  int64_t ntgt = 0;
+  for (int s = 0; s < nseg; ++s) ntgt += segs[s].n;
+  if (ntgt == 0) return;
+  const bool f32 = spec.precision == LPM_FP32C;
+  const int ndim = spec.ndim;
+
+  ctx.arena.reset();
+  // Upper bounds first, so one reservation covers the whole call.
+  NbodyPlan p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
+                           spec.want_psi, ntgt, src.nslots);
+  const size_t rec = f32 ? sizeof(float4) : sizeof(double4);
+  const size_t need = 4096 + sizeof(int) * (2 * size_t(src.nslots) + 2 * (size_t(src.nslots) / SCAN_BLOCK + 2)) +
+                      rec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
+                      sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes() +
+                      sizeof(double) * 1200 + 8 * 256;
+  ctx.arena.reserve(need);
+
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(1, src.nslots)));
+  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(1, src.nslots)));
+  const int64_t nsrc = compact_sources(ctx, src.mask, src.nslots, slot2src, src2slot);
+  p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
+                 spec.want_psi, ntgt, nsrc);
+
+  void* srcp = ctx.arena.take(rec * size_t(p.nsrc_pad));
+  void* tgtp = ctx.arena.take(rec * size_t(p.ntgt_pad));
+  int* tself = static_cast<int*>(ctx.arena.take(sizeof(int) * size_t(p.ntgt_pad)));
+  double* part = static_cast<double*>(ctx.arena.take(p.part_bytes()));
+  double* sgp = static_cast<double*>(ctx.arena.take(sizeof(double) * 1040));
+
+  const int th = 256;
+  {
+    const int64_t nb = (p.nsrc_pad + th - 1) / th;
+    if (f32)
+      k_pack_src<true><<<nb, th, 0, ctx.stream>>>(src2slot, nsrc, p.nsrc_pad, src.x, ndim,
+                                                  src.zeta, src.area, spec.form, srcp);
+    else
+      k_pack_src<false><<<nb, th, 0, ctx.stream>>>(src2slot, nsrc, p.nsrc_pad, src.x, ndim,
+                                                   src.zeta, src.area, spec.form, srcp);
+    ctx.launches++;
+  }
+  int64_t off = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const TgtSeg& g = segs[s];
+    if (g.n > 0) {
+      const int64_t nb = (g.n + th - 1) / th;
+      const int* map = g.collocated ? slot2src : nullptr;
+      const bool skip = g.collocated && spec.skip_self;
+      if (f32)
+        k_pack_tgt<true><<<nb, th, 0, ctx.stream>>>(off, g.n, g.x, ndim, map, skip,
+                                                    src.zeta, src.area, tgtp, tself);
+      else
+        k_pack_tgt<false><<<nb, th, 0, ctx.stream>>>(off, g.n, g.x, ndim, map, skip,
+                                                     src.zeta, src.area, tgtp, tself);
+      ctx.launches++;
+    }
+    off += g.n;
+  }
+  if (p.ntgt_pad > ntgt) {
+    const int64_t nb = (p.ntgt_pad - ntgt + th - 1) / th;
+    k_fill_pad_tgt<<<nb, th, 0, ctx.stream>>>(ntgt, p.ntgt_pad, f32, tgtp, tself);
+    ctx.launches++;
+  }
+  if (f32 && spec.want_psi && ndim == 3) {
+    k_sum_g_partial<<<1024, 256, 0, ctx.stream>>>(static_cast<const float4*>(srcp), nsrc,
+                                                  sgp + 8);
+    k_sum_final<<<1, 32, 0, ctx.stream>>>(sgp + 8, 1024, sgp);
+    ctx.launches += 2;
+  }
+  LPM_CUDA(cudaGetLastError());
+
+  launch_nbody(ctx, p, tgtp, tself, srcp, part, spec.eps);
+
+  const float c0 = f32_c0(ndim, spec.eps);
+  off = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const TgtSeg& g = segs[s];
+    if (g.n > 0) {
+      const float4* t32 = static_cast<const float4*>(tgtp);
+      if (f32) {
+        if (ndim == 3)
+          combine_dispatch<true, 3>(ctx, p, part, off, g, t32, sgp, c0);
+        else
+          combine_dispatch<true, 2>(ctx, p, part, off, g, t32, sgp, c0);
+      } else {
+        if (ndim == 3)
+          combine_dispatch<false, 3>(ctx, p, part, off, g, t32, sgp, c0);
+        else
+          combine_dispatch<false, 2>(ctx, p, part, off, g, t32, sgp, c0);
+      }
+    }
+    off += g.n;
+  }
+  LPM_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------
+// O(N) utilities
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void k_bve_tendency(double* dz, View u, int64_t n, double dt,
+                               double Omega) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dz[i] = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, Omega), u(i, 2)), dt);
+}
+
+__global__ void k_ic2d_tendency(double* dz, View u, int64_t n, int ndim,
+                                double cor) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (ndim == 3)
+    dz[i] = -__dmul_rn(__dmul_rn(2.0, cor), u(i, 2));
+  else
+    dz[i] = -__dmul_rn(cor, u(i, 1));
+}
+
+constexpr int RED_BLOCKS = 512;
+constexpr int RED_THREADS = 256;
+
+// Block-level deterministic reduction of NV values (sum or max per slot).
+template <int NV>
+__device__ void block_reduce(double (&v)[NV], const bool (&is_max)[NV],
+                             double* out) {
+  __shared__ double sh[NV][RED_THREADS];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) sh[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int o = RED_THREADS / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        const double a = sh[k][threadIdx.x], b = sh[k][threadIdx.x + o];
+        sh[k][threadIdx.x] = is_max[k] ? fmax(a, b) : a + b;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] = sh[k][0];
+}
+
+__global__ void k_invariants(int ndim, int64_t n, const double* zeta, View vel,
+                             const double* area, const uint8_t* mask,
+                             double* part) {
+  double v[3] = {0, 0, 0};
+  const bool mx[3] = {false, false, false};
+  for (int64_t i = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS) {
+    if (mask[i]) continue;
+    const double a = area[i];
+    v[0] += zeta[i] * a;
+    v[1] += (zeta[i] * zeta[i]) * a;
+    double n2 = 0;
+    for (int k = 0; k < ndim; ++k) n2 += vel(i, k) * vel(i, k);
+    v[2] += n2 * a;
+  }
+  block_reduce<3>(v, mx, part + 3 * blockIdx.x);
+}
+
+__global__ void k_err(int ndim, int64_t n, View appx, View exact,
+                      const double* wt, const uint8_t* mask, double* part) {
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  const bool mx[6] = {false, false, false, false, true, true};
+  for (int64_t i = (int64_t)blockIdx.x * RED_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * RED_THREADS) {
+    if (mask && mask[i]) continue;
+    double e2 = 0, x2 = 0;
+    for (int k = 0; k < ndim; ++k) {
+      const double e = appx(i, k) - exact(i, k);
+      e2 += e * e;
+      x2 += exact(i, k) * exact(i, k);
+    }
+    const double em = sqrt(e2), xm = sqrt(x2), w = wt ? wt[i] : 1.0;
+    v[0] += em * w;
+    v[1] += xm * w;
+    v[2] += em * em * w;
+    v[3] += xm * xm * w;
+    v[4] = fmax(v[4], em);
+    v[5] = fmax(v[5], xm);
+  }
+  block_reduce<6>(v, mx, part + 6 * blockIdx.x);
+}
+
+template <int NV>
+void finish_reduce(lpm_context& ctx, const double* dpart, double* out,
+                   const bool (&is_max)[NV]) {
+  std::vector<double> h(size_t(NV) * RED_BLOCKS);
+  LPM_CUDA(cudaMemcpyAsync(h.data(), dpart, sizeof(double) * h.size(),
+                           cudaMemcpyDeviceToHost, ctx.stream));
+  LPM_CUDA(cudaStreamSynchronize(ctx.stream));
+  for (int k = 0; k < NV; ++k) out[k] = 0;
+  for (int b = 0; b < RED_BLOCKS; ++b)
+    for (int k = 0; k < NV; ++k)
+      out[k] = is_max[k] ? std::max(out[k], h[NV * b + k]) : out[k] + h[NV * b + k];
+}
+
+template <typename T>
+__global__ void k_fma_peak(T* sink, int iters, T seed) {
+  T a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + T(threadIdx.x + k);
+  const T b = T(0.999999), c = T(1e-7);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == T(-12345.678)) sink[threadIdx.x] = s;
+}
+
+}  // namespace
+
+void bve_tendency(lpm_context& ctx, double* dzeta, View u, int64_t n,
+                  double dt, double Omega) {
+  if (n == 0) return;
+  k_bve_tendency<<<(n + 255) / 256, 256, 0, ctx.stream>>>(dzeta, u, n, dt, Omega);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+void ic2d_tendency(lpm_context& ctx, int ndim, double* dzeta, View u,
+                   int64_t n, double cor) {
+  if (n == 0) return;
+  k_ic2d_tendency<<<(n + 255) / 256, 256, 0, ctx.stream>>>(dzeta, u, n, ndim, cor);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+void invariants(lpm_context& ctx, int ndim, int64_t n, const double* zeta,
+                View vel, const double* area, const uint8_t* mask,
+                double out[3]) {
+  ctx.arena.reset();
+  ctx.arena.reserve(sizeof(double) * 6 * RED_BLOCKS + 256);
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * 3 * RED_BLOCKS));
+  k_invariants<<<RED_BLOCKS, RED_THREADS, 0, ctx.stream>>>(ndim, n, zeta, vel, area,
+                                                           mask, part);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+  const bool mx[3] = {false, false, false};
+  finish_reduce<3>(ctx, part, out, mx);
+  out[1] *= 0.5;
+  out[2] *= 0.5;
+}
+
+void err_norms(lpm_context& ctx, int ndim, int64_t n, View appx, View exact,
+               const double* wt, const uint8_t* mask, double out[3]) {
+  ctx.arena.reset();
+  ctx.arena.reserve(sizeof(double) * 6 * RED_BLOCKS + 256);
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * 6 * RED_BLOCKS));
+  k_err<<<RED_BLOCKS, RED_THREADS, 0, ctx.stream>>>(ndim, n, appx, exact, wt, mask,
+                                                    part);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+  double r[6];
+  const bool mx[6] = {false, false, false, false, true, true};
+  finish_reduce<6>(ctx, part, r, mx);
+  const double tol = 2.220446049250313e-16;
+  auto safe = [tol](double x) { return x / (x * x + tol * tol); };
+  out[0] = r[0] * safe(r[1]);
+  out[1] = std::sqrt(r[2] * safe(r[3]));
+  out[2] = r[4] * safe(r[5]);
+}
+
+double fma_peak(lpm_context& ctx, int precision) {
+  const int blocks = ctx.num_sms * 8, threads = 256;
+  const int iters = precision == LPM_FP32C ? 4096 : 256;
+  ctx.arena.reset();
+  ctx.arena.reserve(4096);
+  void* sink = ctx.arena.take(threads * 8);
+  cudaEvent_t e0, e1;
+  LPM_CUDA(cudaEventCreate(&e0));
+  LPM_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    LPM_CUDA(cudaEventRecord(e0, ctx.stream));
+    if (precision == LPM_FP32C)
+      k_fma_peak<float><<<blocks, threads, 0, ctx.stream>>>(static_cast<float*>(sink), iters, 1.f);
+    else
+      k_fma_peak<double><<<blocks, threads, 0, ctx.stream>>>(static_cast<double*>(sink), iters, 1.0);
+    ctx.launches++;
+    LPM_CUDA(cudaEventRecord(e1, ctx.stream));
+    LPM_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    LPM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * 8 * 16 * double(iters) * blocks * threads;
+  return flops / (best * 1e-3) / 1e12;
+}
+
+}  // namespace lpm

@@ -1,0 +1,168 @@
+// lpm_host.hpp -- internal declarations shared by the library's translation
+// units (not part of the public C ABI, which is include/lpm_gb300.h).
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "lpm_gb300.h"
+
+namespace lpm {
+
+// ---- host-only helpers (mesh.cpp, ics.cpp) --------------------------------
+void mesh_sizes(int kind, int level, int64_t* nv, int64_t* nf);
+void mesh_build(int kind, int level, double radius, double* vx, double* fx,
+                double* farea, uint8_t* fmask);
+void ic_eval(int kind, const double* prm, int np, int ndim, int64_t n,
+             const double* x, double* zeta);
+
+// An error carrying an lpm status code; the C ABI turns it into a return
+// code plus the thread-local message.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+}  // namespace lpm
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+
+namespace lpm {
+
+#define LPM_CUDA(call)                                                    \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess)                                                \
+      throw ::lpm::Error(LPM_ERR_CUDA, std::string(#call) + ": " +        \
+                                           cudaGetErrorString(e_));       \
+  } while (0)
+
+// Strided FP64 view, same layout as lpm_view.
+struct View {
+  double* p;
+  int64_t si;
+  int64_t sc;
+  __host__ __device__ double& operator()(int64_t i, int c) const {
+    return p[i * si + c * sc];
+  }
+};
+inline View to_view(lpm_view v) { return View{v.p, v.stride_i, v.stride_c}; }
+
+// Pair-formula families (arithmetic of the FP64 path).
+enum Form : int {
+  FORM_BVE = 0,    // biot_savart / greens_fn, src/lpm_sphere_functions.hpp
+  FORM_SPHERE = 1, // Incompressible2DKernels<SphereGeometry> (eps form)
+  FORM_PLANE = 2   // Incompressible2DKernels<PlaneGeometry>
+};
+
+// Grow-only device arena owned by a context.
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0;
+  size_t off = 0;
+  void reserve(size_t bytes);
+  void reset() { off = 0; }
+  void* take(size_t bytes) {
+    const size_t a = (off + 255) & ~size_t(255);
+    if (a + bytes > cap) throw Error(LPM_ERR_ALLOC, "arena overflow");
+    off = a + bytes;
+    return base + a;
+  }
+  void release();
+};
+
+}  // namespace lpm
+
+struct lpm_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int precision = LPM_FP64;
+  int num_sms = 0;
+  int* d_err = nullptr;  // device flag: nonzero after a bounded wait gave up
+  lpm::Arena arena;
+  int64_t launches = 0;
+};
+
+namespace lpm {
+
+// Source set: face slots with vorticity, area and the divided-face mask.
+struct SrcSpec {
+  View x;
+  const double* zeta;
+  const double* area;
+  const uint8_t* mask;
+  int64_t nslots;
+};
+
+// One segment of targets (e.g. vertices, or face slots).
+struct TgtSeg {
+  View x;           // positions, rows 0..n-1
+  int64_t n;
+  View u;           // output velocity (u.p may be null)
+  double* psi;      // output stream function (may be null)
+  bool collocated;  // row i is source slot i
+};
+
+struct SumSpec {
+  int ndim;       // 2 plane, 3 sphere
+  int form;       // Form
+  int precision;  // LPM_FP64 or LPM_FP32C
+  double eps;
+  bool want_u;
+  bool want_psi;
+  bool skip_self;  // collocated segments skip their own slot
+};
+
+// Evaluates the direct sum for up to two target segments against one source
+// set, writing into the segments' outputs (asynchronous on ctx.stream).
+void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
+                const TgtSeg* segs, int nseg);
+
+// Source compaction: slot2src[slot] = compacted source index or -1 (masked),
+// src2slot[k] = slot of source k.  Returns the source count (synchronises).
+int64_t compact_sources(lpm_context& ctx, const uint8_t* mask, int64_t nslots,
+                        int* slot2src, int* src2slot);
+
+// Launch plan of the tiled N-body kernels.
+struct NbodyPlan {
+  int precision;
+  int ndim;
+  int form;
+  bool wu, wp;
+  int ncomp;          // partial components per target
+  int64_t ntgt, ntgt_pad;
+  int64_t nsrc, nsrc_pad;
+  int nchunks;
+  int chunk_len;
+  size_t part_bytes() const {
+    return sizeof(double) * size_t(ncomp) * size_t(nchunks) * size_t(ntgt_pad);
+  }
+};
+NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
+                     bool wu, bool wp, int64_t ntgt, int64_t nsrc);
+// tgt: float4[ntgt_pad] (FP32) or double4[ntgt_pad] (FP64, with tself);
+// src: float4/double4[nsrc_pad].  eps: kernel smoothing.
+void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                  const int* tself, const void* src, double* part,
+                  double eps);
+// FP32 squared-distance offset c0 (2 eps^2 on the sphere, eps^2 on the plane,
+// plus the 1e-30 floor).
+float f32_c0(int ndim, double eps);
+
+// Small device utilities (direct_sum.cu).
+void bve_tendency(lpm_context& ctx, double* dzeta, View u, int64_t n,
+                  double dt, double Omega);
+void ic2d_tendency(lpm_context& ctx, int ndim, double* dzeta, View u,
+                   int64_t n, double cor);
+void invariants(lpm_context& ctx, int ndim, int64_t n, const double* zeta,
+                View vel, const double* area, const uint8_t* mask,
+                double out[3]);
+void err_norms(lpm_context& ctx, int ndim, int64_t n, View appx, View exact,
+               const double* wt, const uint8_t* mask, double out[3]);
+double fma_peak(lpm_context& ctx, int precision);
+void check_device_error(lpm_context& ctx);
+
+}  // namespace lpm
+#endif

@@ -1,0 +1,398 @@
+// nbody.cuh -- tiled direct-summation kernels for sm_103a.
+//
+// One CTA owns NT*R targets (R per thread, held in registers) and one chunk
+// of the packed source array.  The chunk streams through shared memory in
+// tiles of TILE sources, double-buffered: one elected thread issues a bulk
+// asynchronous copy (cp.async.bulk, the TMA engine) per tile and the CTA waits
+// on an mbarrier with a bounded spin.  Every thread reads each source record
+// as a shared-memory broadcast and applies it to its R targets.  Each CTA
+// writes one FP64 partial per (chunk, component, target); a combine kernel
+// adds the chunks in fixed order, so results are deterministic.
+//
+// FP32 path (the fast form).  With d = x - y and q = |d|^2 + c0:
+//   sphere: 1 - x.y + eps^2 = q/2 for unit vectors, c0 = 2 eps^2;
+//           x cross y = d cross x, so
+//           u_i = -(1/2pi) (sum_j (g_j/q_j) d_j) cross x_i,
+//           psi_i = -(ln2/4pi) (sum_j g_j lg2 q_j - sum_j g_j)
+//   plane:  c0 = eps^2, u = (-w_1, w_0)/(2pi), psi = -(ln2/4pi) sum g lg2 q
+// with g = zeta*area and w = sum (g/q) d.  Hoisting the cross product out of
+// the sum leaves 10 FP32 operations and one MUFU reciprocal per pair.  c0
+// also carries a 1e-30 floor so a coincident pair (d = 0, the skipped i == j
+// term) contributes exactly 0 to w.  Sums are kept as (S, C) pairs: each
+// tile's plain FP32 partial is merged with an error-free TwoSum, so the
+// compensation costs O(1/TILE) per pair.
+//
+// FP64 path (parity form).  Every pair term is computed with the reference's
+// formula and operation order using non-contracting intrinsics
+// (__dmul_rn/__dadd_rn/__ddiv_rn), so each term equals the reference's term
+// bit for bit; only the grouping of the sum differs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lpm {
+
+constexpr double kPI = 3.1415926535897932384626433832795;
+constexpr double kFOURPI = 4 * kPI;     // 4 * constants::PI
+constexpr double kNEGFOURPI = -4 * kPI;  // -4 * constants::PI
+constexpr double kTWOPI = 2 * kPI;       // 2 * constants::PI
+constexpr float kQFLOOR = 1e-30f;
+
+// Bounded spin limit for mbarrier waits (each try_wait may also suspend in
+// hardware), roughly a second at worst before giving up.
+constexpr unsigned kSpinLimit = 1u << 24;
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+// Bulk (non-tensor) TMA copy global -> shared, completion on an mbarrier.
+// dst/src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src,
+                                            unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Returns false if the phase did not complete within kSpinLimit tries.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar,
+                                                  unsigned parity) {
+  for (unsigned it = 0; it < kSpinLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+  return false;
+}
+
+// Error-free transformation a + b = s + e (Knuth TwoSum), accumulated into
+// the compensation term.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float p) {
+  const float t = s + p;
+  const float bp = t - s;
+  const float e = (s - (t - bp)) + (p - bp);
+  s = t;
+  c += e;
+}
+
+// ---------------------------------------------------------------------------
+// Tile pipeline shared by both precisions.
+// ---------------------------------------------------------------------------
+template <typename Rec, int TILE>
+struct TilePipe {
+  Rec* buf;        // [2][TILE] in shared memory
+  uint64_t* bar;   // [2]
+  const Rec* src;  // chunk start in global memory
+  int ntiles;
+
+  __device__ void start() {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar[0], 1);
+      mbar_init(&bar[1], 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int b = 0; b < 2 && b < ntiles; ++b) issue(b, b);
+    }
+  }
+  __device__ void issue(int tile, int b) {
+    const unsigned bytes = TILE * sizeof(Rec);
+    mbar_expect_tx(&bar[b], bytes);
+    tma_load_1d(buf + b * TILE, src + (int64_t)tile * TILE, bytes, &bar[b]);
+  }
+  // Waits for tile t; returns false (CTA-uniform) if the wait gave up.
+  __device__ bool acquire(int t) {
+    const bool ok = mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1);
+    return !__syncthreads_or(!ok);
+  }
+  // All threads are done with tile t: refill its buffer with tile t + 2.
+  __device__ void release(int t) {
+    __syncthreads();
+    if (threadIdx.x == 0 && t + 2 < ntiles) issue(t + 2, t & 1);
+  }
+  // After a timeout: wait (bounded) for copies still in flight, then return.
+  __device__ void drain(int t, int* err) {
+    if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+      for (int k = t; k < t + 2 && k < ntiles; ++k)
+        (void)mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+    }
+  }
+  __device__ const Rec* tile(int t) const { return buf + (t & 1) * TILE; }
+};
+
+// ---------------------------------------------------------------------------
+// FP32 compensated kernel.
+//   tgt: float4 (x, y, z, unused) per target, ntgt_pad entries
+//   src: float4 (x, y, z, g) per source (plane: z = 0), nsrc_pad entries
+//   part: [chunk][comp][ntgt_pad] doubles; comps = (WU ? NDIM : 0) +
+//         (WP ? 1 : 0): (w0 w1 [w2] [L]) with L = sum g lg2 q
+// ---------------------------------------------------------------------------
+template <int NDIM, bool WU, bool WP, int R, int NT, int TILE>
+__global__ void __launch_bounds__(NT)
+    nbody_f32(const float4* __restrict__ tgt, const float4* __restrict__ src,
+              int64_t ntgt_pad, int64_t nsrc_pad, int chunk_len, float c0,
+              double* __restrict__ part, int* err) {
+  constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
+  __shared__ __align__(128) float4 sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+
+  const int tid = threadIdx.x;
+  const int64_t tbase = (int64_t)blockIdx.x * (NT * R);
+  const int64_t s0 = (int64_t)blockIdx.y * chunk_len;
+  int64_t slen = nsrc_pad - s0;
+  if (slen > chunk_len) slen = chunk_len;
+
+  float tx[R], ty[R], tz[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float4 t = tgt[tbase + r * NT + tid];
+    tx[r] = t.x;
+    ty[r] = t.y;
+    tz[r] = t.z;
+  }
+  float S[NC][R], C[NC][R];
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      S[k][r] = 0.f;
+      C[k][r] = 0.f;
+    }
+
+  TilePipe<float4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  pipe.start();
+  for (int t = 0; t < pipe.ntiles; ++t) {
+    if (!pipe.acquire(t)) {
+      pipe.drain(t, err);
+      return;
+    }
+    const float4* sm = pipe.tile(t);
+    float P[NC][R];
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+      for (int r = 0; r < R; ++r) P[k][r] = 0.f;
+
+#pragma unroll 4
+    for (int j = 0; j < TILE; ++j) {
+      const float4 s = sm[j];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float dx = tx[r] - s.x;
+        const float dy = ty[r] - s.y;
+        float q;
+        float dz = 0.f;
+        if (NDIM == 3) {
+          dz = tz[r] - s.z;
+          q = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, c0)));
+        } else {
+          q = fmaf(dx, dx, fmaf(dy, dy, c0));
+        }
+        if (WU) {
+          const float w = s.w * rcp_approx(q);
+          P[0][r] = fmaf(w, dx, P[0][r]);
+          P[1][r] = fmaf(w, dy, P[1][r]);
+          if (NDIM == 3) P[2][r] = fmaf(w, dz, P[2][r]);
+        }
+        if (WP) {
+          P[NC - 1][r] = fmaf(s.w, lg2_approx(q), P[NC - 1][r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+#pragma unroll
+      for (int r = 0; r < R; ++r) two_sum_acc(S[k][r], C[k][r], P[k][r]);
+    pipe.release(t);
+  }
+
+  double* out = part + (int64_t)blockIdx.y * NC * ntgt_pad;
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+      out[k * ntgt_pad + tbase + r * NT + tid] =
+          (double)S[k][r] + (double)C[k][r];
+}
+
+// ---------------------------------------------------------------------------
+// FP64 parity kernel.
+//   tgt:  double4 (x, y, z, unused) per target
+//   tself: per-target source index to skip (-1 = none)
+//   src:  double4 (x, y, z, g): g = (-zeta)*area for FORM_BVE (the reference's
+//         circ), zeta*area otherwise
+//   part: [chunk][comp][ntgt_pad]; comps = (WU ? NDIM : 0) + (WP ? 1 : 0)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dmul(double a, double b) {
+  return __dmul_rn(a, b);
+}
+__device__ __forceinline__ double dadd(double a, double b) {
+  return __dadd_rn(a, b);
+}
+__device__ __forceinline__ double dsub(double a, double b) {
+  return __dsub_rn(a, b);
+}
+__device__ __forceinline__ double ddiv(double a, double b) {
+  return __ddiv_rn(a, b);
+}
+
+template <int FORM, bool WU, bool WP, int R, int NT, int TILE>
+__global__ void __launch_bounds__(NT)
+    nbody_f64(const double4* __restrict__ tgt, const int* __restrict__ tself,
+              const double4* __restrict__ src, int64_t ntgt_pad,
+              int64_t nsrc_pad, int chunk_len, double eps2,
+              double* __restrict__ part, int* err) {
+  constexpr int ND = (FORM == 2) ? 2 : 3;
+  constexpr int NC = (WU ? ND : 0) + (WP ? 1 : 0);
+  __shared__ __align__(128) double4 sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+
+  const int tid = threadIdx.x;
+  const int64_t tbase = (int64_t)blockIdx.x * (NT * R);
+  const int64_t s0 = (int64_t)blockIdx.y * chunk_len;
+  int64_t slen = nsrc_pad - s0;
+  if (slen > chunk_len) slen = chunk_len;
+
+  double x0[R], x1[R], x2[R];
+  int self[R];
+  double A[NC][R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int64_t ti = tbase + r * NT + tid;
+    const double4 t = tgt[ti];
+    x0[r] = t.x;
+    x1[r] = t.y;
+    x2[r] = t.z;
+    self[r] = tself[ti];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) A[k][r] = 0.0;
+  }
+
+  TilePipe<double4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  pipe.start();
+  for (int t = 0; t < pipe.ntiles; ++t) {
+    if (!pipe.acquire(t)) {
+      pipe.drain(t, err);
+      return;
+    }
+    const double4* sm = pipe.tile(t);
+    const int jbase = int(s0 + (int64_t)t * TILE);
+#pragma unroll 1
+    for (int j = 0; j < TILE; ++j) {
+      const double4 s = sm[j];
+      const int jg = jbase + j;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const bool skip = (jg == self[r]);
+        if (FORM == 0) {
+          // biot_savart / greens_fn (src/lpm_sphere_functions.hpp:21-57)
+          const double dt =
+              dadd(dadd(dmul(x0[r], s.x), dmul(x1[r], s.y)), dmul(x2[r], s.z));
+          const double omd = dsub(1.0, dt);
+          if (WU) {
+            const double c0 = dsub(dmul(x1[r], s.z), dmul(x2[r], s.y));
+            const double c1 = dsub(dmul(x2[r], s.x), dmul(x0[r], s.z));
+            const double c2 = dsub(dmul(x0[r], s.y), dmul(x1[r], s.x));
+            const double st = ddiv(s.w, dmul(kFOURPI, omd));
+            A[0][r] = dadd(A[0][r], skip ? 0.0 : dmul(c0, st));
+            A[1][r] = dadd(A[1][r], skip ? 0.0 : dmul(c1, st));
+            A[2][r] = dadd(A[2][r], skip ? 0.0 : dmul(c2, st));
+          }
+          if (WP) {
+            const double p = ddiv(dmul(log(omd), s.w), kFOURPI);
+            A[NC - 1][r] = dadd(A[NC - 1][r], skip ? 0.0 : p);
+          }
+        } else if (FORM == 1) {
+          // Incompressible2DKernels<SphereGeometry>::kernel_vals
+          // (src/lpm_incompressible2d_kernels.hpp:35-47)
+          const double dt =
+              dadd(dadd(dmul(x0[r], s.x), dmul(x1[r], s.y)), dmul(x2[r], s.z));
+          const double arg = dadd(dsub(1.0, dt), eps2);
+          if (WU) {
+            const double den = dmul(kNEGFOURPI, arg);
+            const double c0 = dsub(dmul(x1[r], s.z), dmul(x2[r], s.y));
+            const double c1 = dsub(dmul(x2[r], s.x), dmul(x0[r], s.z));
+            const double c2 = dsub(dmul(x0[r], s.y), dmul(x1[r], s.x));
+            A[0][r] = dadd(A[0][r], skip ? 0.0 : dmul(ddiv(c0, den), s.w));
+            A[1][r] = dadd(A[1][r], skip ? 0.0 : dmul(ddiv(c1, den), s.w));
+            A[2][r] = dadd(A[2][r], skip ? 0.0 : dmul(ddiv(c2, den), s.w));
+          }
+          if (WP) {
+            const double p = dmul(ddiv(-log(arg), kFOURPI), s.w);
+            A[NC - 1][r] = dadd(A[NC - 1][r], skip ? 0.0 : p);
+          }
+        } else {
+          // Incompressible2DKernels<PlaneGeometry>::kernel_vals (:72-84)
+          const double m0 = dsub(x0[r], s.x);
+          const double m1 = dsub(x1[r], s.y);
+          const double arg = dadd(dadd(dmul(m0, m0), dmul(m1, m1)), eps2);
+          if (WU) {
+            const double den = dmul(kTWOPI, arg);
+            A[0][r] = dadd(A[0][r], skip ? 0.0 : dmul(ddiv(-m1, den), s.w));
+            A[1][r] = dadd(A[1][r], skip ? 0.0 : dmul(ddiv(m0, den), s.w));
+          }
+          if (WP) {
+            const double p = dmul(ddiv(-log(arg), kFOURPI), s.w);
+            A[NC - 1][r] = dadd(A[NC - 1][r], skip ? 0.0 : p);
+          }
+        }
+      }
+    }
+    pipe.release(t);
+  }
+
+  double* out = part + (int64_t)blockIdx.y * NC * ntgt_pad;
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[k * ntgt_pad + tbase + r * NT + tid] = A[k][r];
+}
+
+// Launch shapes.  FP32: 256 threads x 4 targets, 512-source tiles (8 KB per
+// buffer).  FP64: 128 threads x 2 targets, 256-source tiles (8 KB).
+constexpr int F32_NT = 256, F32_R = 4, F32_TILE = 512;
+constexpr int F64_NT = 128, F64_R = 2, F64_TILE = 256;
+
+}  // namespace lpm

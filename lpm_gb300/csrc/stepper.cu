@@ -1,0 +1,725 @@
+// stepper.cu -- device-resident time steppers.
+//
+// BVERK4::advance_timestep (src/lpm_bve_rk4_impl.hpp:63-167) runs, per step,
+// 4 direct-sum evaluations plus ~30 BLAS-1 / tendency launches.  Here every
+// O(N) operation between two evaluations is fused into the epilogue that
+// combines the previous evaluation's partial sums: it writes the velocity,
+// forms the stage increments (KokkosBlas::scal, BVEVorticityTendency), the
+// next stage's work positions and vorticity (KokkosBlas::update), and packs
+// the next evaluation's source and target tiles.  A step is then
+//   begin, [nbody, stage] x 3, nbody, final
+// = 9 kernels, captured once into a CUDA graph and replayed.
+//
+// All state updates are FP64 with non-contracting intrinsics in the
+// reference's operation order; only the pair sums use the FP32 form when the
+// stepper runs in LPM_FP32C.
+//
+// Incompressible2DRK2::advance_timestep_impl
+// (src/lpm_incompressible2d_rk2_impl.hpp:74-172) is fused the same way:
+//   begin, nbody, mid, nbody, final.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lpm_host.hpp"
+#include "nbody.cuh"
+
+namespace lpm {
+namespace {
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+
+// Device view of the stepper's targets: vertices first, then face targets
+// (all face slots, or the unmasked ones with LPM_STEP_SKIP_MASKED_TARGETS).
+struct Tg {
+  int ndim;
+  int64_t nv, T;
+  const int* fslot;     // face target -> face slot
+  const int* slot2src;  // face slot -> source index or -1
+  View vx, fx, vvel, fvel;
+  double *vzeta, *fzeta, *vpsi, *fpsi;
+  const double* farea;
+  __device__ bool face(int64_t t) const { return t >= nv; }
+  __device__ int64_t slot(int64_t t) const { return fslot[t - nv]; }
+  __device__ double& x(int64_t t, int c) const {
+    return face(t) ? fx(slot(t), c) : vx(t, c);
+  }
+  __device__ double& u(int64_t t, int c) const {
+    return face(t) ? fvel(slot(t), c) : vvel(t, c);
+  }
+  __device__ double& zeta(int64_t t) const {
+    return face(t) ? fzeta[slot(t)] : vzeta[t];
+  }
+  __device__ double* psi(int64_t t) const {
+    return face(t) ? (fpsi ? fpsi + slot(t) : nullptr) : (vpsi ? vpsi + t : nullptr);
+  }
+};
+
+// Packed tiles and partials of the stepper's evaluations.
+struct Pk {
+  bool f32;
+  int form;
+  bool skip_self;
+  void* tgt;
+  int* tself;
+  void* src;
+  const double* part;
+  int nchunks;
+  int64_t tpad;
+  const float* sg;  // unused placeholder for alignment
+};
+
+// Pack target t (and its source record when it is an unmasked face) at
+// position p with vorticity z.
+__device__ void pack(const Tg& g, const Pk& k, int64_t t, const double* p,
+                     double z) {
+  int src = -1;
+  double area = 0.0;
+  if (g.face(t)) {
+    const int64_t s = g.slot(t);
+    src = g.slot2src[s];
+    area = g.farea[s];
+  }
+  const double p2 = g.ndim == 3 ? p[2] : 0.0;
+  if (k.f32) {
+    const float gw = src >= 0 ? __double2float_rn(dm(z, area)) : 0.f;
+    const float4 r = make_float4(__double2float_rn(p[0]), __double2float_rn(p[1]),
+                                 __double2float_rn(p2), gw);
+    static_cast<float4*>(k.tgt)[t] =
+        make_float4(r.x, r.y, r.z, (k.skip_self && src >= 0) ? gw : 0.f);
+    if (src >= 0) static_cast<float4*>(k.src)[src] = r;
+  } else {
+    static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, 0.0);
+    k.tself[t] = (k.skip_self && src >= 0) ? src : -1;
+    if (src >= 0) {
+      const double gg = (k.form == FORM_BVE) ? dm(-z, area) : dm(z, area);
+      static_cast<double4*>(k.src)[src] = make_double4(p[0], p[1], p2, gg);
+    }
+  }
+}
+
+// Sum of the chunk partials of target t.  FP32: converts w into u (and the
+// log sum into psi) with the FP64 position p at which t was evaluated.
+__device__ void combine(const Tg& g, const Pk& k, int64_t t, const double* p,
+                        bool wp, float c0, const double* sg, double* u,
+                        double* psi) {
+  const int nd = g.ndim;
+  const int nc = nd + (wp ? 1 : 0);
+  double a[4] = {0, 0, 0, 0};
+  for (int c = 0; c < k.nchunks; ++c) {
+    const double* q = k.part + (int64_t)c * nc * k.tpad + t;
+    for (int m = 0; m < nc; ++m) a[m] += q[m * k.tpad];
+  }
+  if (!k.f32) {
+    for (int m = 0; m < nd; ++m) u[m] = a[m];
+    if (wp) *psi = a[nd];
+    return;
+  }
+  constexpr double INV2PI = 1.0 / (2.0 * kPI);
+  constexpr double LN2_4PI = 0.69314718055994530942 / (4.0 * kPI);
+  if (nd == 3) {
+    u[0] = -INV2PI * (a[1] * p[2] - a[2] * p[1]);
+    u[1] = -INV2PI * (a[2] * p[0] - a[0] * p[2]);
+    u[2] = -INV2PI * (a[0] * p[1] - a[1] * p[0]);
+  } else {
+    u[0] = -INV2PI * a[1];
+    u[1] = INV2PI * a[0];
+  }
+  if (wp) {
+    const float gs = static_cast<const float4*>(k.tgt)[t].w;
+    double L = a[nd] - (double)gs * (double)lg2_approx(c0);
+    if (nd == 3) L -= (*sg - (double)gs);
+    *psi = -LN2_4PI * L;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// BVE RK4
+// ---------------------------------------------------------------------------
+struct Rk4Buf {
+  double* xs[4];  // stage increments x_s = dt*u, SoA [3][T]
+  double* zs[4];  // stage vorticity increments [T]
+  double* xw;     // current evaluation positions, SoA [3][T]
+};
+
+struct Rk4Par {
+  double dt, Omega;
+  bool fix_facevort3, reproject;
+  float c0;
+};
+
+__device__ __forceinline__ double bve_tend(double uz, double dt, double Om) {
+  return dm(dm(dm(-2.0, Om), uz), dt);
+}
+
+// Stage 1 increments from the entry velocities, then stage-2 work state.
+__global__ void k_rk4_begin(Tg g, Pk k, Rk4Buf b, Rk4Par P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int64_t T = g.T;
+  double p[3];
+  for (int c = 0; c < 3; ++c) {
+    const double x1 = dm(P.dt, g.u(t, c));
+    b.xs[0][c * T + t] = x1;
+    p[c] = da(g.x(t, c), dm(0.5, x1));
+    b.xw[c * T + t] = p[c];
+  }
+  const double z1 = bve_tend(g.u(t, 2), P.dt, P.Omega);
+  b.zs[0][t] = z1;
+  pack(g, k, t, p, da(g.zeta(t), dm(0.5, z1)));
+}
+
+// After evaluation s (1..3): store velocity, increments of stage s+1 and the
+// work state of the next evaluation; after s == 3 apply BVERK4Update.
+__global__ void k_rk4_stage(Tg g, Pk k, Rk4Buf b, Rk4Par P, int s) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int64_t T = g.T;
+  double pw[3], u[3];
+  for (int c = 0; c < 3; ++c) pw[c] = b.xw[c * T + t];
+  combine(g, k, t, pw, false, P.c0, nullptr, u, nullptr);
+  for (int c = 0; c < 3; ++c) {
+    g.u(t, c) = u[c];
+    b.xs[s][c * T + t] = dm(P.dt, u[c]);
+  }
+  const double zsv = bve_tend(u[2], P.dt, P.Omega);
+  b.zs[s][t] = zsv;
+  double p[3];
+  double z;
+  if (s < 3) {
+    const double cf = (s == 1) ? 0.5 : 1.0;
+    for (int c = 0; c < 3; ++c) {
+      p[c] = da(g.x(t, c), dm(cf, b.xs[s][c * T + t]));
+      b.xw[c * T + t] = p[c];
+    }
+    z = da(g.zeta(t), dm(cf, zsv));
+  } else {
+    constexpr double sixth = 1.0 / 6.0;
+    constexpr double third = 1.0 / 3.0;
+    for (int c = 0; c < 3; ++c) {
+      const double inc = da(dm(sixth, da(b.xs[0][c * T + t], b.xs[3][c * T + t])),
+                            dm(third, da(b.xs[1][c * T + t], b.xs[2][c * T + t])));
+      p[c] = da(g.x(t, c), inc);
+    }
+    if (P.reproject) {
+      const double r = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+      for (int c = 0; c < 3; ++c) p[c] = p[c] / r;
+    }
+    for (int c = 0; c < 3; ++c) {
+      g.x(t, c) = p[c];
+      b.xw[c * T + t] = p[c];
+    }
+    // the reference passes facevort4 for facevort3 in the face update
+    const double z3 = (g.face(t) && !P.fix_facevort3) ? b.zs[3][t] : b.zs[2][t];
+    const double zinc = da(dm(sixth, da(b.zs[0][t], b.zs[3][t])),
+                           dm(third, da(b.zs[1][t], z3)));
+    z = da(g.zeta(t), zinc);
+    g.zeta(t) = z;
+  }
+  pack(g, k, t, p, z);
+}
+
+__global__ void k_rk4_final(Tg g, Pk k, Rk4Buf b, Rk4Par P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int64_t T = g.T;
+  double pw[3], u[3];
+  for (int c = 0; c < 3; ++c) pw[c] = b.xw[c * T + t];
+  combine(g, k, t, pw, false, P.c0, nullptr, u, nullptr);
+  for (int c = 0; c < 3; ++c) g.u(t, c) = u[c];
+}
+
+// ---------------------------------------------------------------------------
+// incompressible2d RK2 (Heun)
+// ---------------------------------------------------------------------------
+struct Rk2Buf {
+  double* x1;  // SoA [ndim][T]
+  double* z1;  // [T]
+  double* xw;  // SoA [ndim][T]
+};
+struct Rk2Par {
+  double dt, cor;
+  float c0;
+  const double* sg;  // device: sum of source strengths (FP32 sphere psi)
+};
+
+__device__ __forceinline__ double ic2d_tend(int nd, const double* u, double cor) {
+  return nd == 3 ? -dm(dm(2.0, cor), u[2]) : -dm(cor, u[1]);
+}
+
+__global__ void k_rk2_begin(Tg g, Pk k, Rk2Buf b, Rk2Par P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int nd = g.ndim;
+  const int64_t T = g.T;
+  double u[3] = {0, 0, 0}, p[3] = {0, 0, 0};
+  for (int c = 0; c < nd; ++c) u[c] = g.u(t, c);
+  for (int c = 0; c < nd; ++c) {
+    b.x1[c * T + t] = dm(P.dt, u[c]);
+    p[c] = da(g.x(t, c), dm(P.dt, u[c]));
+    b.xw[c * T + t] = p[c];
+  }
+  const double z1 = ic2d_tend(nd, u, P.cor);
+  b.z1[t] = z1;
+  pack(g, k, t, p, da(g.zeta(t), dm(P.dt, z1)));
+}
+
+__global__ void k_rk2_mid(Tg g, Pk k, Rk2Buf b, Rk2Par P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int nd = g.ndim;
+  const int64_t T = g.T;
+  double pw[3] = {0, 0, 0}, u[3] = {0, 0, 0}, ps = 0;
+  for (int c = 0; c < nd; ++c) pw[c] = b.xw[c * T + t];
+  combine(g, k, t, pw, true, P.c0, P.sg, u, &ps);
+  for (int c = 0; c < nd; ++c) g.u(t, c) = u[c];
+  if (double* pp = g.psi(t)) *pp = ps;
+  const double z2 = ic2d_tend(nd, u, P.cor);
+  const double h = dm(0.5, P.dt);
+  const double z = da(da(dm(h, b.z1[t]), dm(h, z2)), g.zeta(t));
+  g.zeta(t) = z;
+  double p[3] = {0, 0, 0};
+  for (int c = 0; c < nd; ++c) {
+    const double x2 = dm(P.dt, u[c]);
+    p[c] = da(da(dm(0.5, b.x1[c * T + t]), dm(0.5, x2)), g.x(t, c));
+    g.x(t, c) = p[c];
+    b.xw[c * T + t] = p[c];
+  }
+  pack(g, k, t, p, z);
+}
+
+__global__ void k_rk2_final(Tg g, Pk k, Rk2Buf b, Rk2Par P) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.T) return;
+  const int nd = g.ndim;
+  const int64_t T = g.T;
+  double pw[3] = {0, 0, 0}, u[3] = {0, 0, 0}, ps = 0;
+  for (int c = 0; c < nd; ++c) pw[c] = b.xw[c * T + t];
+  combine(g, k, t, pw, true, P.c0, P.sg, u, &ps);
+  for (int c = 0; c < nd; ++c) g.u(t, c) = u[c];
+  if (double* pp = g.psi(t)) *pp = ps;
+}
+
+__global__ void k_zero_bytes(char* p, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+}
+
+__global__ void k_face_targets(const uint8_t* mask, int64_t nf, bool skip,
+                               const int* slot2src, int* fslot) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nf) return;
+  if (!skip) {
+    fslot[s] = int(s);
+  } else {
+    const int k = slot2src[s];
+    if (k >= 0) fslot[k] = int(s);
+  }
+}
+
+// Deterministic sum of packed FP32 source strengths into *out.
+__global__ void k_sg_partial(const float4* src, int64_t n, double* part) {
+  __shared__ double sh[256];
+  double s = 0;
+  for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * 256)
+    s += (double)src[i].w;
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+__global__ void k_sg_final(const double* part, int n, double* out) {
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += part[i];
+    *out = s;
+  }
+}
+
+}  // namespace
+}  // namespace lpm
+
+// ---------------------------------------------------------------------------
+// Common stepper state
+// ---------------------------------------------------------------------------
+struct lpm_stepper_base {
+  lpm_context* ctx = nullptr;
+  int ndim = 3;
+  int64_t nv = 0, nf = 0;
+  double dt = 0, eps = 0;
+  int precision = LPM_FP64;
+  uint32_t flags = 0;
+  int form = lpm::FORM_BVE;
+  bool skip_self = true;
+  bool want_psi = false;
+
+  bool ready = false;
+  int64_t nsrc = 0, nft = 0, T = 0;
+  lpm::NbodyPlan plan{};
+  std::vector<void*> allocs;
+  int *slot2src = nullptr, *src2slot = nullptr, *fslot = nullptr, *tself = nullptr;
+  void *tgt = nullptr, *src = nullptr;
+  double* part = nullptr;
+  double* sgbuf = nullptr;  // [0] = sum, [8..] partials
+
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<char> key;
+  int64_t graph_kernels = 0;
+
+  void* dalloc(size_t bytes) {
+    void* p = nullptr;
+    LPM_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+    allocs.push_back(p);
+    return p;
+  }
+  void free_all() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    cap_stream = nullptr;
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+  }
+
+  // Maps, packed buffers and the launch plan; run once (the mask is fixed).
+  void setup(const uint8_t* fmask) {
+    lpm_context& c = *ctx;
+    slot2src = static_cast<int*>(dalloc(sizeof(int) * nf));
+    src2slot = static_cast<int*>(dalloc(sizeof(int) * nf));
+    c.arena.reset();
+    c.arena.reserve(sizeof(int) * (2 * size_t(nf) / 1024 + 8) + 4096);
+    nsrc = lpm::compact_sources(c, fmask, nf, slot2src, src2slot);
+    const bool skip_masked = flags & LPM_STEP_SKIP_MASKED_TARGETS;
+    nft = skip_masked ? nsrc : nf;
+    T = nv + nft;
+    fslot = static_cast<int*>(dalloc(sizeof(int) * std::max<int64_t>(nft, 1)));
+    if (nf > 0) {
+      lpm::k_face_targets<<<(nf + 255) / 256, 256, 0, c.stream>>>(fmask, nf, skip_masked,
+                                                                  slot2src, fslot);
+      c.launches++;
+    }
+    plan = lpm::plan_nbody(c, precision, ndim, form, true, want_psi, T, nsrc);
+    const size_t rec = precision == LPM_FP32C ? 16 : 32;
+    tgt = dalloc(rec * plan.ntgt_pad);
+    src = dalloc(rec * plan.nsrc_pad);
+    tself = static_cast<int*>(dalloc(sizeof(int) * plan.ntgt_pad));
+    part = static_cast<double*>(dalloc(plan.part_bytes()));
+    sgbuf = static_cast<double*>(dalloc(sizeof(double) * (8 + 256)));
+    // zero the padding records once (never rewritten); tself padding = -1
+    zero(tgt, rec * plan.ntgt_pad);
+    zero(src, rec * plan.nsrc_pad);
+    LPM_CUDA(cudaMemsetAsync(tself, 0xff, sizeof(int) * plan.ntgt_pad, c.stream));
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    LPM_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    ready = true;
+  }
+  void zero(void* p, size_t n) {
+    lpm::k_zero_bytes<<<(n + 255) / 256, 256, 0, ctx->stream>>>(static_cast<char*>(p), n);
+    ctx->launches++;
+  }
+
+  lpm::Tg targets(lpm_view vx, double* vzeta, lpm_view vvel, double* vpsi,
+                  lpm_view fx, double* fzeta, lpm_view fvel, double* fpsi,
+                  const double* farea) const {
+    lpm::Tg g;
+    g.ndim = ndim;
+    g.nv = nv;
+    g.T = T;
+    g.fslot = fslot;
+    g.slot2src = slot2src;
+    g.vx = lpm::to_view(vx);
+    g.fx = lpm::to_view(fx);
+    g.vvel = lpm::to_view(vvel);
+    g.fvel = lpm::to_view(fvel);
+    g.vzeta = vzeta;
+    g.fzeta = fzeta;
+    g.vpsi = vpsi;
+    g.fpsi = fpsi;
+    g.farea = farea;
+    return g;
+  }
+  lpm::Pk packs() const {
+    lpm::Pk k;
+    k.f32 = precision == LPM_FP32C;
+    k.form = form;
+    k.skip_self = skip_self;
+    k.tgt = tgt;
+    k.tself = tself;
+    k.src = src;
+    k.part = part;
+    k.nchunks = plan.nchunks;
+    k.tpad = plan.ntgt_pad;
+    k.sg = nullptr;
+    return k;
+  }
+  void nbody() {
+    if (precision == LPM_FP32C && want_psi && ndim == 3) {
+      lpm::k_sg_partial<<<256, 256, 0, ctx->stream>>>(static_cast<const float4*>(src),
+                                                      nsrc, sgbuf + 8);
+      lpm::k_sg_final<<<1, 32, 0, ctx->stream>>>(sgbuf + 8, 256, sgbuf);
+      ctx->launches += 2;
+    }
+    lpm::launch_nbody(*ctx, plan, tgt, tself, src, part, eps);
+  }
+
+  // Runs `body` either directly or through a graph captured for this key.
+  template <typename F>
+  void run(const std::vector<char>& k, F body) {
+    lpm_context& c = *ctx;
+    if (flags & LPM_STEP_NO_GRAPH) {
+      body();
+      LPM_CUDA(cudaGetLastError());
+      return;
+    }
+    if (!exec || k != key) {
+      if (exec) cudaGraphExecDestroy(exec);
+      exec = nullptr;
+      cudaStream_t user = c.stream;
+      const int64_t before = c.launches;
+      // order the capture after prior work on the user's stream
+      LPM_CUDA(cudaStreamSynchronize(user));
+      c.stream = cap_stream;
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        try {
+          body();
+        } catch (...) {
+          cudaStreamEndCapture(cap_stream, &graph);
+          if (graph) cudaGraphDestroy(graph);
+          c.stream = user;
+          throw;
+        }
+        e = cudaStreamEndCapture(cap_stream, &graph);
+      }
+      c.stream = user;
+      LPM_CUDA(e);
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      LPM_CUDA(e);
+      graph_kernels = c.launches - before;
+      c.launches = before;
+      key = k;
+    }
+    LPM_CUDA(cudaGraphLaunch(exec, c.stream));
+    c.launches += graph_kernels;
+  }
+};
+
+struct lpm_bve_rk4 : lpm_stepper_base {
+  double Omega = 0;
+  double* buf = nullptr;  // xs[4], zs[4], xw
+
+  void advance(lpm_view vx, double* vzeta, lpm_view vvel, lpm_view fx,
+               double* fzeta, lpm_view fvel, const double* farea,
+               const uint8_t* fmask) {
+    if (!ready) {
+      setup(fmask);
+      buf = static_cast<double*>(dalloc(sizeof(double) * size_t(T) * (4 * 3 + 4 + 3)));
+    }
+    lpm::Tg g = targets(vx, vzeta, vvel, nullptr, fx, fzeta, fvel, nullptr, farea);
+    lpm::Pk k = packs();
+    lpm::Rk4Buf b;
+    for (int s = 0; s < 4; ++s) {
+      b.xs[s] = buf + size_t(T) * 3 * s;
+      b.zs[s] = buf + size_t(T) * 12 + size_t(T) * s;
+    }
+    b.xw = buf + size_t(T) * 16;
+    lpm::Rk4Par P;
+    P.dt = dt;
+    P.Omega = Omega;
+    P.fix_facevort3 = flags & LPM_STEP_FIX_FACEVORT3;
+    P.reproject = flags & LPM_STEP_REPROJECT;
+    P.c0 = lpm::f32_c0(3, eps);
+
+    std::vector<char> kk(sizeof(lpm::Tg));
+    std::memcpy(kk.data(), &g, sizeof(g));
+    const int64_t nb = (T + 255) / 256;
+    run(kk, [&]() {
+      if (T == 0) return;
+      lpm::k_rk4_begin<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
+      ctx->launches++;
+      for (int s = 1; s <= 3; ++s) {
+        nbody();
+        lpm::k_rk4_stage<<<nb, 256, 0, ctx->stream>>>(g, k, b, P, s);
+        ctx->launches++;
+      }
+      nbody();
+      lpm::k_rk4_final<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
+      ctx->launches++;
+    });
+  }
+};
+
+struct lpm_ic2d_rk2 : lpm_stepper_base {
+  double cor = 0;
+  double* buf = nullptr;
+
+  void advance(lpm_view vx, double* vzeta, lpm_view vvel, double* vpsi,
+               lpm_view fx, double* fzeta, lpm_view fvel, double* fpsi,
+               const double* farea, const uint8_t* fmask) {
+    if (!ready) {
+      setup(fmask);
+      buf = static_cast<double*>(dalloc(sizeof(double) * size_t(T) * (2 * ndim + 1)));
+    }
+    lpm::Tg g = targets(vx, vzeta, vvel, vpsi, fx, fzeta, fvel, fpsi, farea);
+    lpm::Pk k = packs();
+    lpm::Rk2Buf b;
+    b.x1 = buf;
+    b.z1 = buf + size_t(T) * ndim;
+    b.xw = buf + size_t(T) * (ndim + 1);
+    lpm::Rk2Par P;
+    P.dt = dt;
+    P.cor = cor;
+    P.c0 = lpm::f32_c0(ndim, eps);
+    P.sg = sgbuf;
+    std::vector<char> kk(sizeof(lpm::Tg));
+    std::memcpy(kk.data(), &g, sizeof(g));
+    const int64_t nb = (T + 255) / 256;
+    run(kk, [&]() {
+      if (T == 0) return;
+      lpm::k_rk2_begin<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
+      ctx->launches++;
+      nbody();
+      lpm::k_rk2_mid<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
+      ctx->launches++;
+      nbody();
+      lpm::k_rk2_final<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
+      ctx->launches++;
+    });
+  }
+};
+
+// ---------------------------------------------------------------------------
+// C ABI of the steppers (the rest of the ABI is in capi.cu)
+// ---------------------------------------------------------------------------
+namespace lpm {
+int fail(int code, const char* msg);  // capi.cu
+int handle_exception();               // capi.cu
+}
+
+extern "C" {
+
+int lpm_bve_rk4_create(lpm_context* ctx, lpm_bve_rk4** out, int64_t nverts,
+                       int64_t nfaces, double dt, double Omega, double eps,
+                       int precision, uint32_t flags) {
+  try {
+    if (!ctx || !out) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: null argument");
+    if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
+      return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: sizes out of range");
+    if (precision != LPM_FP64 && precision != LPM_FP32C)
+      return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: precision must be LPM_FP64 or LPM_FP32C");
+    if (!std::isfinite(dt) || !std::isfinite(Omega) || !std::isfinite(eps) || eps < 0)
+      return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: non-finite dt/Omega or bad eps");
+    auto* st = new lpm_bve_rk4();
+    st->ctx = ctx;
+    st->ndim = 3;
+    st->nv = nverts;
+    st->nf = nfaces;
+    st->dt = dt;
+    st->Omega = Omega;
+    st->eps = eps;
+    st->precision = precision;
+    st->flags = flags;
+    st->form = eps == 0.0 ? lpm::FORM_BVE : lpm::FORM_SPHERE;
+    st->skip_self = true;  // BVE face functors always skip i == j
+    st->want_psi = false;
+    *out = st;
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_bve_rk4_destroy(lpm_bve_rk4* st) {
+  if (!st) return LPM_OK;
+  st->free_all();
+  delete st;
+  return LPM_OK;
+}
+
+int lpm_bve_rk4_advance_timestep(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
+                                 lpm_view vvel, lpm_view fx, double* fzeta,
+                                 lpm_view fvel, const double* farea,
+                                 const uint8_t* fmask) {
+  try {
+    if (!st) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_advance_timestep: null stepper");
+    if ((st->nv > 0 && (!vx.p || !vzeta || !vvel.p)) ||
+        (st->nf > 0 && (!fx.p || !fzeta || !fvel.p || !farea || !fmask)))
+      return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_advance_timestep: null array");
+    cudaSetDevice(st->ctx->device);
+    st->advance(vx, vzeta, vvel, fx, fzeta, fvel, farea, fmask);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_ic2d_rk2_create(lpm_context* ctx, lpm_ic2d_rk2** out, int ndim,
+                        int64_t nverts, int64_t nfaces, double dt, double eps,
+                        double cor, int precision, uint32_t flags) {
+  try {
+    if (!ctx || !out) return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: null argument");
+    if (ndim != LPM_SPHERE && ndim != LPM_PLANE)
+      return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: ndim must be 2 or 3");
+    if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
+      return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: sizes out of range");
+    if (precision != LPM_FP64 && precision != LPM_FP32C)
+      return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: bad precision");
+    if (!std::isfinite(dt) || !std::isfinite(cor) || !std::isfinite(eps) || eps < 0)
+      return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: non-finite dt/cor or bad eps");
+    auto* st = new lpm_ic2d_rk2();
+    st->ctx = ctx;
+    st->ndim = ndim;
+    st->nv = nverts;
+    st->nf = nfaces;
+    st->dt = dt;
+    st->eps = eps;
+    st->cor = cor;
+    st->precision = precision;
+    st->flags = flags;
+    st->form = ndim == 3 ? lpm::FORM_SPHERE : lpm::FORM_PLANE;
+    // Incompressible2DActiveSums: skip i == j only when eps is zero (:235)
+    st->skip_self = (std::fabs(eps) < 2.220446049250313e-16) ||
+                    (flags & LPM_STEP_SKIP_SELF_ALWAYS);
+    st->want_psi = true;
+    *out = st;
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_ic2d_rk2_destroy(lpm_ic2d_rk2* st) {
+  if (!st) return LPM_OK;
+  st->free_all();
+  delete st;
+  return LPM_OK;
+}
+
+int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
+                                  double* vzeta, lpm_view vvel, double* vpsi,
+                                  lpm_view fx, double* fzeta, lpm_view fvel,
+                                  double* fpsi, const double* farea,
+                                  const uint8_t* fmask) {
+  try {
+    if (!st) return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_advance_timestep: null stepper");
+    if ((st->nv > 0 && (!vx.p || !vzeta || !vvel.p)) ||
+        (st->nf > 0 && (!fx.p || !fzeta || !fvel.p || !farea || !fmask)))
+      return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_advance_timestep: null array");
+    cudaSetDevice(st->ctx->device);
+    st->advance(vx, vzeta, vvel, vpsi, fx, fzeta, fvel, fpsi, farea, fmask);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+}  // extern "C"

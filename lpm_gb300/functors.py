@@ -1,0 +1,110 @@
+"""One call per reference Kokkos functor launch on the direct-sum path.
+
+Each function takes device tensors (torch, on the context's GPU) with the
+reference functor's argument meaning and launches the matching CUDA path:
+
+=========================  =====================================================
+function                   reference (pbosler/lpm)
+=========================  =====================================================
+bve_vertex_solve           BVEVertexSolve   src/lpm_bve_sphere_kernels.hpp:90
+bve_vertex_stream_fn       BVEVertexStreamFn                          :141
+bve_vertex_velocity        BVEVertexVelocity                          :179
+bve_face_solve             BVEFaceSolve                               :284
+bve_face_stream_fn         BVEFaceStreamFn                            :329
+bve_face_velocity          BVEFaceVelocity                            :365
+bve_vorticity_tendency     BVEVorticityTendency                       :399
+ic2d_passive_sums          Incompressible2DPassiveSums  src/lpm_incompressible2d_kernels.hpp:144
+ic2d_active_sums           Incompressible2DActiveSums                 :201
+ic2d_tendencies            Incompressible2DTendencies                 :257
+=========================  =====================================================
+
+``nsrc`` / ``n_active`` is the number of face slots (all tree levels); the
+mask excludes divided faces.  Arithmetic follows ``ctx.precision``.
+"""
+from __future__ import annotations
+
+from .core import check, lib, ptr, view, View
+
+
+def _n(t):
+    return 0 if t is None else int(t.shape[0])
+
+
+def bve_vertex_solve(ctx, psi, u, vx, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_vertex_solve(ctx.handle, ptr(psi), view(u), view(vx), _n(vx), view(fx),
+                                     ptr(zeta), ptr(area), ptr(mask), nsrc))
+
+
+def bve_vertex_stream_fn(ctx, psi, vx, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_vertex_stream_fn(ctx.handle, ptr(psi), view(vx), _n(vx), view(fx),
+                                         ptr(zeta), ptr(area), ptr(mask), nsrc))
+
+
+def bve_vertex_velocity(ctx, u, vx, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_vertex_velocity(ctx.handle, view(u), view(vx), _n(vx), view(fx),
+                                        ptr(zeta), ptr(area), ptr(mask), nsrc))
+
+
+def bve_face_solve(ctx, psi, u, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_face_solve(ctx.handle, ptr(psi), view(u), view(fx), ptr(zeta),
+                                   ptr(area), ptr(mask), nsrc))
+
+
+def bve_face_stream_fn(ctx, psi, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_face_stream_fn(ctx.handle, ptr(psi), view(fx), ptr(zeta), ptr(area),
+                                       ptr(mask), nsrc))
+
+
+def bve_face_velocity(ctx, u, fx, zeta, area, mask, nsrc=None):
+    nsrc = _n(fx) if nsrc is None else nsrc
+    check(lib().lpm_bve_face_velocity(ctx.handle, view(u), view(fx), ptr(zeta), ptr(area),
+                                      ptr(mask), nsrc))
+
+
+def bve_vorticity_tendency(ctx, dzeta, u, dt, Omega):
+    check(lib().lpm_bve_vorticity_tendency(ctx.handle, ptr(dzeta), view(u), _n(u), dt, Omega))
+
+
+def ic2d_passive_sums(ctx, u, psi, x, y, zeta, area, mask, eps, n_active=None):
+    ndim = int(x.shape[1])
+    n_active = _n(y) if n_active is None else n_active
+    check(lib().lpm_ic2d_passive_sums(ctx.handle, ndim, view(u), ptr(psi), view(x), _n(x),
+                                      view(y), ptr(zeta), ptr(area), ptr(mask), eps, n_active))
+
+
+def ic2d_active_sums(ctx, u, psi, xy, zeta, area, mask, eps, n_active=None, self_rule=0):
+    ndim = int(xy.shape[1])
+    n_active = _n(xy) if n_active is None else n_active
+    check(lib().lpm_ic2d_active_sums(ctx.handle, ndim, view(u), ptr(psi), view(xy), ptr(zeta),
+                                     ptr(area), ptr(mask), eps, n_active, self_rule))
+
+
+def ic2d_tendencies(ctx, dzeta, u, cor):
+    check(lib().lpm_ic2d_tendencies(ctx.handle, int(u.shape[1]), ptr(dzeta), view(u), _n(u), cor))
+
+
+def ic2d_invariants(ctx, zeta, vel, area, mask):
+    import ctypes as C
+    out = (C.c_double * 3)()
+    check(lib().lpm_ic2d_invariants(ctx.handle, int(vel.shape[1]), _n(zeta), ptr(zeta), view(vel),
+                                    ptr(area), ptr(mask), out))
+    return tuple(out)
+
+
+def err_norms(ctx, appx, exact, wt=None, mask=None):
+    """ErrNorms (src/lpm_error.hpp:81-91): (l1, l2, linf)."""
+    import ctypes as C
+    out = (C.c_double * 3)()
+    a = appx if appx.dim() == 2 else appx.reshape(-1, 1)
+    e = exact if exact.dim() == 2 else exact.reshape(-1, 1)
+    check(lib().lpm_err_norms(ctx.handle, int(a.shape[1]), _n(a), view(a), view(e), ptr(wt),
+                              ptr(mask), out))
+    return tuple(out)
+
+
+__all__ = [n for n in dir() if not n.startswith("_") and n not in ("check", "lib", "ptr", "view", "View")]

@@ -1,0 +1,188 @@
+"""TEST INFRASTRUCTURE ONLY: numpy binding of the FP64 CPU oracle
+(oracle/lpm_oracle.cpp).  Imported by the tests, the smoke check and the
+CPU-baseline leg of bench.py as the checker; never by the product path.
+
+Parity status: partially pinned (see the header of lpm_oracle.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "build" / "liblpm_oracle.so"
+
+_lib = None
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "lpm_oracle.cpp").stat().st_mtime:
+            build()
+        L = C.CDLL(str(LIB))
+        vp, l, i, d = C.c_void_p, C.c_long, C.c_int, C.c_double
+        sig = {
+            "oracle_set_threads": [i],
+            "oracle_max_threads": [],
+            "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
+            "oracle_bve_face_solve": [vp, vp, l, vp, vp, vp, vp, vp, l, i],
+            "oracle_ic2d_passive_sums": [i, vp, vp, vp, l, vp, vp, vp, vp, vp, d, l, i],
+            "oracle_ic2d_active_sums": [i, vp, vp, l, vp, vp, vp, vp, vp, d, l, i, i],
+            "oracle_bve_rk4_step": [l, vp, vp, vp, l, vp, vp, vp, vp, vp, d, d, d, i, i],
+            "oracle_ic2d_init_direct_sums": [i, l, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, i],
+            "oracle_ic2d_rk2_step": [i, l, vp, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, d, i],
+            "oracle_invariants": [i, l, vp, vp, vp, vp, vp],
+            "oracle_err_norms": [i, l, vp, vp, vp, vp, vp],
+        }
+        for k, a in sig.items():
+            f = getattr(L, k)
+            f.argtypes = a
+            f.restype = C.c_int if k == "oracle_max_threads" else None
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f(a, shape=None):
+    a = np.ascontiguousarray(a, np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def bve_vertex_solve(vx, fx, zeta, area, mask, want_u=True, want_psi=True, tgt_idx=None,
+                     compensated=False):
+    """BVEVertexSolve: returns (psi, u) over targets (tgt_idx subset if given)."""
+    vx, fx, zeta, area = _f(vx), _f(fx), _f(zeta), _f(area)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    idx = None if tgt_idx is None else np.ascontiguousarray(tgt_idx, np.int64)
+    n = vx.shape[0] if idx is None else idx.shape[0]
+    psi = np.zeros(n) if want_psi else None
+    u = np.zeros((n, 3)) if want_u else None
+    lib().oracle_bve_vertex_solve(_p(psi), _p(u), _p(vx), n, _p(idx), _p(fx), _p(zeta), _p(area),
+                                  _p(mask), fx.shape[0], int(compensated))
+    return psi, u
+
+
+def bve_face_solve(fx, zeta, area, mask, want_u=True, want_psi=True, tgt_idx=None,
+                   compensated=False):
+    fx, zeta, area = _f(fx), _f(zeta), _f(area)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    idx = None if tgt_idx is None else np.ascontiguousarray(tgt_idx, np.int64)
+    n = fx.shape[0] if idx is None else idx.shape[0]
+    psi = np.zeros(n) if want_psi else None
+    u = np.zeros((n, 3)) if want_u else None
+    lib().oracle_bve_face_solve(_p(psi), _p(u), n, _p(idx), _p(fx), _p(zeta), _p(area), _p(mask),
+                                fx.shape[0], int(compensated))
+    return psi, u
+
+
+def ic2d_passive_sums(x, y, zeta, area, mask, eps, tgt_idx=None, compensated=False):
+    x, y, zeta, area = _f(x), _f(y), _f(zeta), _f(area)
+    ndim = x.shape[1]
+    mask = np.ascontiguousarray(mask, np.uint8)
+    idx = None if tgt_idx is None else np.ascontiguousarray(tgt_idx, np.int64)
+    n = x.shape[0] if idx is None else idx.shape[0]
+    u, psi = np.zeros((n, ndim)), np.zeros(n)
+    lib().oracle_ic2d_passive_sums(ndim, _p(u), _p(psi), _p(x), n, _p(idx), _p(y), _p(zeta),
+                                   _p(area), _p(mask), float(eps), y.shape[0], int(compensated))
+    return u, psi
+
+
+def ic2d_active_sums(y, zeta, area, mask, eps, self_rule=0, tgt_idx=None, compensated=False):
+    y, zeta, area = _f(y), _f(zeta), _f(area)
+    ndim = y.shape[1]
+    mask = np.ascontiguousarray(mask, np.uint8)
+    idx = None if tgt_idx is None else np.ascontiguousarray(tgt_idx, np.int64)
+    n = y.shape[0] if idx is None else idx.shape[0]
+    u, psi = np.zeros((n, ndim)), np.zeros(n)
+    lib().oracle_ic2d_active_sums(ndim, _p(u), _p(psi), n, _p(idx), _p(y), _p(zeta), _p(area),
+                                  _p(mask), float(eps), y.shape[0], int(self_rule),
+                                  int(compensated))
+    return u, psi
+
+
+class BVEState:
+    """Host copy of a BVE state advanced by the oracle's BVERK4."""
+
+    def __init__(self, vx, vzeta, vvel, fx, fzeta, fvel, farea, fmask):
+        self.vx, self.vzeta, self.vvel = _f(vx).copy(), _f(vzeta).copy(), _f(vvel).copy()
+        self.fx, self.fzeta, self.fvel = _f(fx).copy(), _f(fzeta).copy(), _f(fvel).copy()
+        self.farea = _f(farea)
+        self.fmask = np.ascontiguousarray(fmask, np.uint8)
+
+    def step(self, dt, Omega, eps=0.0, fix_facevort3=False, reproject=False):
+        lib().oracle_bve_rk4_step(self.vx.shape[0], _p(self.vx), _p(self.vzeta), _p(self.vvel),
+                                  self.fx.shape[0], _p(self.fx), _p(self.fzeta), _p(self.fvel),
+                                  _p(self.farea), _p(self.fmask), float(dt), float(Omega),
+                                  float(eps), int(fix_facevort3), int(reproject))
+
+
+class IC2DState:
+    """Host copy of an incompressible2d state advanced by the oracle's RK2."""
+
+    def __init__(self, vx, vzeta, fx, fzeta, farea, fmask, eps, cor, self_rule=0):
+        self.ndim = np.asarray(vx).shape[1]
+        self.vx, self.vzeta = _f(vx).copy(), _f(vzeta).copy()
+        self.fx, self.fzeta = _f(fx).copy(), _f(fzeta).copy()
+        self.farea = _f(farea)
+        self.fmask = np.ascontiguousarray(fmask, np.uint8)
+        self.eps, self.cor, self.self_rule = float(eps), float(cor), int(self_rule)
+        nv, nf, nd = self.vx.shape[0], self.fx.shape[0], self.ndim
+        self.vvel, self.vpsi = np.zeros((nv, nd)), np.zeros(nv)
+        self.fvel, self.fpsi = np.zeros((nf, nd)), np.zeros(nf)
+
+    def init_direct_sums(self):
+        lib().oracle_ic2d_init_direct_sums(self.ndim, self.vx.shape[0], _p(self.vx), _p(self.vvel),
+                                           _p(self.vpsi), self.fx.shape[0], _p(self.fx),
+                                           _p(self.fzeta), _p(self.fvel), _p(self.fpsi),
+                                           _p(self.farea), _p(self.fmask), self.eps,
+                                           self.self_rule)
+
+    def step(self, dt):
+        lib().oracle_ic2d_rk2_step(self.ndim, self.vx.shape[0], _p(self.vx), _p(self.vzeta),
+                                   _p(self.vvel), _p(self.vpsi), self.fx.shape[0], _p(self.fx),
+                                   _p(self.fzeta), _p(self.fvel), _p(self.fpsi), _p(self.farea),
+                                   _p(self.fmask), float(dt), self.eps, self.cor, self.self_rule)
+
+
+def invariants(zeta, vel, area, mask):
+    zeta, vel, area = _f(zeta), _f(vel), _f(area)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros(3)
+    lib().oracle_invariants(vel.shape[1], zeta.shape[0], _p(zeta), _p(vel), _p(area), _p(mask),
+                            _p(out))
+    return tuple(out)
+
+
+def err_norms(appx, exact, wt=None, mask=None):
+    """ErrNorms: (l1, l2, linf) of vector magnitudes or scalars."""
+    a = _f(appx)
+    e = _f(exact)
+    if a.ndim == 1:
+        a, e = a.reshape(-1, 1), e.reshape(-1, 1)
+    w = None if wt is None else _f(wt)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros(3)
+    lib().oracle_err_norms(a.shape[1], a.shape[0], _p(a), _p(e), _p(w), _p(m), _p(out))
+    return tuple(out)

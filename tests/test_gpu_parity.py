@@ -1,0 +1,212 @@
+"""CUDA path vs the FP64 CPU oracle on the same inputs (run with -m gpu).
+
+Tolerances (relative to the largest reference magnitude, the ErrNorms linf
+normalisation of src/lpm_error.hpp:81-91):
+  FP64 path   1e-12 (each pair term is bit-identical; only sum grouping differs)
+  FP32C path  2e-6 velocity, 2e-6 stream function on leaf targets
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from lpm_gb300 import core
+from lpm_gb300 import functors as F
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-6
+OMEGA = 2 * math.pi
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.abs(b).max()
+    return np.abs(a - b).max() / (den if den > 0 else 1.0)
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def sphere_case(level, seed=core.MESH_ICOS_TRI, kind=core.IC_RH54, params=None, noise=0.0):
+    vx, fx, fa, fm = core.build_mesh(seed, level, 1.0)
+    if params is None:
+        w = OMEGA / 12.5
+        params = (w, -w)
+    zf = core.eval_ic(kind, params, fx)
+    if noise:
+        zf = zf + noise * np.random.default_rng(7).standard_normal(zf.shape)
+    return vx, fx, fa, fm, zf
+
+
+@pytest.mark.parametrize("level", [0, 2, 3])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP32C])
+def test_bve_functors(gpu_ctx, oracle, level, precision):
+    ctx = gpu_ctx
+    ctx.set_precision(precision)
+    vx, fx, fa, fm, zf = sphere_case(level, noise=0.5)
+    psi_v, u_v = oracle.bve_vertex_solve(vx, fx, zf, fa, fm)
+    psi_f, u_f = oracle.bve_face_solve(fx, zf, fa, fm)
+    dvx, dfx, dz, da, dm = dev(vx), dev(fx), dev(zf), dev(fa), dev(fm)
+    gu = torch.zeros(vx.shape[0], 3, dtype=torch.float64, device="cuda")
+    gp = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
+    F.bve_vertex_solve(ctx, gp, gu, dvx, dfx, dz, da, dm)
+    gfu = torch.zeros(fx.shape[0], 3, dtype=torch.float64, device="cuda")
+    gfp = torch.zeros(fx.shape[0], dtype=torch.float64, device="cuda")
+    F.bve_face_solve(ctx, gfp, gfu, dfx, dz, da, dm)
+    ctx.synchronize()
+    leaf = fm == 0
+    if precision == core.FP64:
+        assert rel(gu.cpu(), u_v) < TOL64
+        assert rel(gp.cpu(), psi_v) < TOL64
+        assert rel(gfu.cpu(), u_f) < TOL64
+        assert rel(gfp.cpu(), psi_f) < TOL64
+    else:
+        assert rel(gu.cpu(), u_v) < TOL32
+        assert rel(gp.cpu(), psi_v) < TOL32
+        assert rel(gfu.cpu().numpy()[leaf], u_f[leaf]) < TOL32
+        assert rel(gfp.cpu().numpy()[leaf], psi_f[leaf]) < TOL32
+    # velocity-only and stream-function-only launches give the same values
+    gu2 = torch.zeros_like(gu)
+    F.bve_vertex_velocity(ctx, gu2, dvx, dfx, dz, da, dm)
+    gp2 = torch.zeros_like(gp)
+    F.bve_vertex_stream_fn(ctx, gp2, dvx, dfx, dz, da, dm)
+    gfu2 = torch.zeros_like(gfu)
+    F.bve_face_velocity(ctx, gfu2, dfx, dz, da, dm)
+    gfp2 = torch.zeros_like(gfp)
+    F.bve_face_stream_fn(ctx, gfp2, dfx, dz, da, dm)
+    ctx.synchronize()
+    assert torch.equal(gu2, gu) and torch.equal(gfu2, gfu)
+    tolp = 0 if precision == core.FP64 else 1e-12
+    assert rel(gp2.cpu(), gp.cpu()) <= tolp and rel(gfp2.cpu(), gfp.cpu()) <= tolp
+
+
+def test_bve_soa_layout(gpu_ctx, oracle):
+    """LayoutLeft (SoA, stride = nmax) views give the same answer as AoS."""
+    ctx = gpu_ctx
+    ctx.set_precision(core.FP64)
+    vx, fx, fa, fm, zf = sphere_case(3)
+    nmax_v, nmax_f = vx.shape[0] + 5, fx.shape[0] + 3
+    soa_v = torch.zeros(3, nmax_v, dtype=torch.float64, device="cuda")
+    soa_v[:, : vx.shape[0]] = dev(vx).T
+    soa_f = torch.zeros(3, nmax_f, dtype=torch.float64, device="cuda")
+    soa_f[:, : fx.shape[0]] = dev(fx).T
+    vview = soa_v[:, : vx.shape[0]].T  # stride (1, nmax)
+    fview = soa_f[:, : fx.shape[0]].T
+    assert vview.stride() == (1, nmax_v)
+    u_soa = torch.zeros(3, nmax_v, dtype=torch.float64, device="cuda")
+    F.bve_vertex_velocity(ctx, u_soa[:, : vx.shape[0]].T, vview, fview, dev(zf), dev(fa), dev(fm))
+    _, u_ref = oracle.bve_vertex_solve(vx, fx, zf, fa, fm, want_psi=False)
+    ctx.synchronize()
+    assert rel(u_soa[:, : vx.shape[0]].T.cpu(), u_ref) < TOL64
+
+
+@pytest.mark.parametrize("eps", [0.0, 0.05])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP32C])
+@pytest.mark.parametrize("geom", ["sphere", "plane"])
+def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
+    ctx = gpu_ctx
+    ctx.set_precision(precision)
+    if geom == "sphere":
+        vx, fx, fa, fm, zf = sphere_case(3, seed=core.MESH_CUBED_SPHERE,
+                                         kind=core.IC_GAUSSIAN_SPHERE,
+                                         params=(4 * math.pi, 4.0, 0.0, math.pi / 20, 0.0, 0.0))
+    else:
+        vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 4, 4.0)
+        zf = core.eval_ic(core.IC_DIPOLE_PAIR, (2.0, 1.0, -2.0, 0.0, -2.0, 1.0, 2.0, 0.0), fx)
+    nd = vx.shape[1]
+    u_p, psi_p = oracle.ic2d_passive_sums(vx, fx, zf, fa, fm, eps)
+    u_a, psi_a = oracle.ic2d_active_sums(fx, zf, fa, fm, eps)
+    gu = torch.zeros(vx.shape[0], nd, dtype=torch.float64, device="cuda")
+    gp = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
+    fu = torch.zeros(fx.shape[0], nd, dtype=torch.float64, device="cuda")
+    fp = torch.zeros(fx.shape[0], dtype=torch.float64, device="cuda")
+    dfx, dz, da, dm = dev(fx), dev(zf), dev(fa), dev(fm)
+    F.ic2d_passive_sums(ctx, gu, gp, dev(vx), dfx, dz, da, dm, eps)
+    F.ic2d_active_sums(ctx, fu, fp, dfx, dz, da, dm, eps)
+    ctx.synchronize()
+    leaf = fm == 0
+    tol = TOL64 if precision == core.FP64 else TOL32
+    assert rel(gu.cpu(), u_p) < tol
+    assert rel(gp.cpu(), psi_p) < tol
+    sel = slice(None) if precision == core.FP64 else leaf
+    assert rel(fu.cpu().numpy()[sel], u_a[sel]) < tol
+    assert rel(fp.cpu().numpy()[sel], psi_a[sel]) < tol
+
+
+@pytest.mark.parametrize("precision", [core.FP64, core.FP32C])
+def test_edge_cases(gpu_ctx, oracle, precision):
+    ctx = gpu_ctx
+    ctx.set_precision(precision)
+    vx, fx, fa, fm, zf = sphere_case(1)
+    dfx, dz, da = dev(fx), dev(zf), dev(fa)
+    # every face masked: no sources, all sums zero
+    allm = torch.ones(fx.shape[0], dtype=torch.uint8, device="cuda")
+    u = torch.full((vx.shape[0], 3), 7.0, dtype=torch.float64, device="cuda")
+    F.bve_vertex_velocity(ctx, u, dev(vx), dfx, dz, da, allm)
+    ctx.synchronize()
+    assert torch.count_nonzero(u) == 0
+    # a single target, a single unmasked source
+    one = np.ones(fx.shape[0], np.uint8)
+    one[fx.shape[0] - 1] = 0
+    u1 = torch.zeros(1, 3, dtype=torch.float64, device="cuda")
+    F.bve_vertex_velocity(ctx, u1, dev(vx[:1]), dfx, dz, da, dev(one))
+    _, ur = oracle.bve_vertex_solve(vx[:1], fx, zf, fa, one, want_psi=False)
+    ctx.synchronize()
+    assert rel(u1.cpu(), ur) < (TOL64 if precision == core.FP64 else TOL32)
+    # zero targets: no launch, no error
+    u0 = torch.zeros(0, 3, dtype=torch.float64, device="cuda")
+    F.bve_vertex_velocity(ctx, u0, dev(vx[:0]), dfx, dz, da, dev(fm))
+    ctx.synchronize()
+
+
+def test_determinism(gpu_ctx):
+    ctx = gpu_ctx
+    for precision in (core.FP64, core.FP32C):
+        ctx.set_precision(precision)
+        vx, fx, fa, fm, zf = sphere_case(4)
+        outs = []
+        for _ in range(2):
+            u = torch.zeros(fx.shape[0], 3, dtype=torch.float64, device="cuda")
+            F.bve_face_velocity(ctx, u, dev(fx), dev(zf), dev(fa), dev(fm))
+            outs.append(u)
+        ctx.synchronize()
+        assert torch.equal(outs[0], outs[1])
+
+
+def test_argument_errors(gpu_ctx):
+    ctx = gpu_ctx
+    L = core.lib()
+    nullv = core.View(None, 0, 0)
+    rc = L.lpm_bve_vertex_velocity(ctx.handle, nullv, nullv, 10, nullv, None, None, None, 10)
+    assert rc == core.LPM_ERR_ARG
+    assert b"null" in L.lpm_last_error()
+    rc = L.lpm_context_set_precision(ctx.handle, 16)
+    assert rc == core.LPM_ERR_ARG
+    with pytest.raises(core.LpmError):
+        core.check(L.lpm_ic2d_passive_sums(ctx.handle, 4, nullv, None, nullv, 0, nullv, None, None,
+                                           None, 0.0, 0))
+
+
+def test_tendencies_and_invariants(gpu_ctx, oracle):
+    ctx = gpu_ctx
+    vx, fx, fa, fm, zf = sphere_case(3)
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((fx.shape[0], 3))
+    dz = torch.zeros(fx.shape[0], dtype=torch.float64, device="cuda")
+    F.bve_vorticity_tendency(ctx, dz, dev(u), 0.01, OMEGA)
+    ctx.synchronize()
+    assert np.array_equal(dz.cpu().numpy(), -2.0 * OMEGA * u[:, 2] * 0.01)
+    F.ic2d_tendencies(ctx, dz, dev(u), OMEGA)
+    ctx.synchronize()
+    assert np.array_equal(dz.cpu().numpy(), -(2 * OMEGA * u[:, 2]))
+    inv = F.ic2d_invariants(ctx, dev(zf), dev(u), dev(fa), dev(fm))
+    ref = oracle.invariants(zf, u, fa, fm)
+    assert np.allclose(inv, ref, rtol=1e-12, atol=0)
+    en = F.err_norms(ctx, dev(u + 1e-3), dev(u), dev(fa), dev(fm))
+    er = oracle.err_norms(u + 1e-3, u, fa, fm)
+    assert np.allclose(en, er, rtol=1e-12)
