@@ -1,0 +1,480 @@
+"""Benchmark of the BVE RK4 direct-sum path on GB300.
+
+Workload (default, the metric's configuration): barotropic vorticity on the
+unit sphere, icosahedral level 7 (327,680 leaf faces = sources, 163,842
+vertices = passive targets), Gaussian vortex 4 pi exp(-(1 - x.x0)/0.25^2)
+centred at lat 0.05 pi, lon 0, plus 2 Omega z, Omega = 2 pi, smoothing
+eps = 0.01, RK4 with dt = 0.005.  A step is one RK4 step: four direct-sum
+evaluations over (vertices + leaf faces) x leaf faces.  Inputs are synthetic
+(the mesh and the vorticity are generated, no dataset is read).
+
+Interactions are counted as in the metric: (Nv + Nf) * Nf per evaluation, Nf =
+leaf faces.  `value` uses the FP32-compensated path with inputs resident in
+HBM; the FP64 path (reference arithmetic) is reported beside it, as are the
+relative errors of the FP32 path against FP64 on the same state.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BVE RK4 Ginteractions/s: plain FP64 vs FP32-comp/learned at equal L∞ error"
+UNIT = "Ginteractions/s"
+LEVEL = 7
+EPS = 0.01
+DT = 0.005
+OMEGA = 2 * math.pi
+FLOPS_PER_PAIR = 24  # credited flops of the sphere u pair (eps form)
+L2_FLUSH_BYTES = 512 << 20
+
+
+def workload_config(level: int, nv: int, nf: int) -> dict:
+    return {
+        "workload": f"BVE sphere icosahedral level {level} RK4, Gaussian vortex + 2*Omega*z, "
+                    f"eps={EPS}, dt={DT}",
+        "level": level, "vertices": nv, "leaf_faces": nf, "eps": EPS, "dt": DT,
+        "interactions_per_step": 4 * (nv + nf) * nf,
+        "l2": "flushed between timed steps (512 MiB write)",
+        "parallelism": "replicas (one independent problem per GPU)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for name, v in zip(names, s[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+# ---------------------------------------------------------------------------
+# workload setup
+# ---------------------------------------------------------------------------
+def make_state(level: int):
+    from lpm_gb300 import core
+
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
+    params = (4 * math.pi, 4.0, 0.0, 0.05 * math.pi, 0.0, OMEGA)
+    vz = core.eval_ic(core.IC_GAUSSIAN_SPHERE, params, vx)
+    fz = core.eval_ic(core.IC_GAUSSIAN_SPHERE, params, fx)
+    return vx, fx, fa, fm, vz, fz
+
+
+class DeviceState:
+    def __init__(self, host, device):
+        import torch
+
+        vx, fx, fa, fm, vz, fz = host
+        d = torch.device("cuda", device)
+        self.vx = torch.from_numpy(vx).to(d)
+        self.fx = torch.from_numpy(fx).to(d)
+        self.fa = torch.from_numpy(fa).to(d)
+        self.fm = torch.from_numpy(fm).to(d)
+        self.vz = torch.from_numpy(vz).to(d)
+        self.fz = torch.from_numpy(fz).to(d)
+        self.vu = torch.zeros_like(self.vx)
+        self.fu = torch.zeros_like(self.fx)
+
+    def clone(self):
+        c = DeviceState.__new__(DeviceState)
+        for k, v in self.__dict__.items():
+            setattr(c, k, v.clone())
+        return c
+
+    def velocity(self, ctx, precision):
+        """Velocities of the current state (eps sphere kernel, faces skip i == j)."""
+        from lpm_gb300 import functors as F
+
+        ctx.set_precision(precision)
+        F.ic2d_passive_sums(ctx, self.vu, None, self.vx, self.fx, self.fz, self.fa, self.fm, EPS)
+        F.ic2d_active_sums(ctx, self.fu, None, self.fx, self.fz, self.fa, self.fm, EPS,
+                           self_rule=1)
+
+
+def make_stepper(ctx, st, precision, flags):
+    import ctypes as C
+
+    from lpm_gb300 import core
+
+    h = C.c_void_p()
+    core.check(core.lib().lpm_bve_rk4_create(ctx.handle, C.byref(h), st.vx.shape[0],
+                                             st.fx.shape[0], DT, OMEGA, EPS, precision, flags))
+    return h
+
+
+def advance(h, st):
+    from lpm_gb300 import core
+    from lpm_gb300.core import ptr, view
+
+    core.check(core.lib().lpm_bve_rk4_advance_timestep(
+        h, view(st.vx), ptr(st.vz), view(st.vu), view(st.fx), ptr(st.fz), view(st.fu),
+        ptr(st.fa), ptr(st.fm)))
+
+
+def rel_errors(got, ref, mask=None):
+    import torch
+
+    g = got if got.dim() == 2 else got.reshape(-1, 1)
+    r = ref if ref.dim() == 2 else ref.reshape(-1, 1)
+    if mask is not None:
+        keep = mask == 0
+        g, r = g[keep], r[keep]
+    em = torch.linalg.norm(g - r, dim=1)
+    xm = torch.linalg.norm(r, dim=1)
+    return {"linf": float(em.max() / xm.max()), "l2": float(torch.sqrt((em ** 2).sum() / (xm ** 2).sum()))}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, device):
+    import torch
+    import torch.distributed as dist
+
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+
+    host = make_state(args.level)
+    vx, fx, fa, fm, vz, fz = host
+    nv, nleaf = vx.shape[0], int((fm == 0).sum())
+    ipe = (nv + nleaf) * nleaf  # interactions per evaluation
+    base = DeviceState(host, device)
+    base.velocity(ctx, core.FP32C)
+    torch.cuda.synchronize(device)
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # ---- headline: FP32C stepper, graph-replayed, inputs resident ----------
+    # FP64 position update with reprojection onto the sphere; divided parent
+    # slots (which nothing reads) are neither evaluated nor moved.
+    st = base.clone()
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+    h = make_stepper(ctx, st, core.FP32C, flags)
+    for _ in range(args.warmup):
+        advance(h, st)
+    torch.cuda.synchronize(device)
+    barrier()
+    sampler = ClockSampler(device) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    launches0 = ctx.kernel_launches
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize(device)
+    barrier()
+    for k in range(args.steps):
+        flush.fill_(float(k))  # evict L2 between timed steps (untimed)
+        ev[k][0].record(stream)
+        advance(h, st)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(device)
+    barrier()
+    clocks = sampler.stop() if sampler else None
+    launches = ctx.kernel_launches - launches0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * 4 * ipe * args.steps / (ms * 1e-3) / 1e9
+    core.lib().lpm_bve_rk4_destroy(h)
+
+    result = {}
+    if rank == 0:
+        # ---- kernel timing for the roofline (events around each N-body) ----
+        st2 = base.clone()
+        h2 = make_stepper(ctx, st2, core.FP32C, flags | core.STEP_TIME_NBODY)
+        advance(h2, st2)  # warm
+        import ctypes as C
+        msn, nn = C.c_double(), C.c_int64()
+        core.check(core.lib().lpm_bve_rk4_nbody_time(h2, C.byref(msn), C.byref(nn)))
+        for _ in range(2):
+            flush.fill_(1.0)
+            advance(h2, st2)
+        core.check(core.lib().lpm_bve_rk4_nbody_time(h2, C.byref(msn), C.byref(nn)))
+        core.lib().lpm_bve_rk4_destroy(h2)
+        nbody_ms = msn.value / max(nn.value, 1)
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+            if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+        nsm = torch.cuda.get_device_properties(device).multi_processor_count
+        peak_fp32 = 2 * 128 * nsm * sm_max * 1e6 / 1e12
+        achieved = ipe * FLOPS_PER_PAIR / (nbody_ms * 1e-3) / 1e12
+        traffic = None
+        tf = ROOT / "profiles" / "roofline_traffic.json"
+        if tf.exists():
+            try:
+                traffic = json.loads(tf.read_text()).get("nbody_f32_sphere_u_bytes_per_launch")
+            except Exception:
+                traffic = None
+        fma32 = ctx.fma_peak_tflops(core.FP32C)
+        fma64 = ctx.fma_peak_tflops(core.FP64)
+
+        # ---- accuracy 1: one evaluation on the initial (unit-sphere) state,
+        # FP32C vs the reference's FP64 arithmetic; also the FP64 throughput ----
+        s64 = base.clone()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s64.velocity(ctx, core.FP64)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms64_eval = e0.elapsed_time(e1)
+        e_v = rel_errors(base.vu, s64.vu)
+        e_f = rel_errors(base.fu, s64.fu, base.fm)
+
+        # ---- accuracy 2: one RK4 step, FP32C vs the same algorithm in FP64
+        # (chord form, LPM_FP64_CHORD), same flags; also its throughput ----
+        sa, sb = base.clone(), base.clone()
+        ha = make_stepper(ctx, sa, core.FP32C, flags | core.STEP_NO_GRAPH)
+        hb = make_stepper(ctx, sb, core.FP64_CHORD, flags | core.STEP_NO_GRAPH)
+        advance(ha, sa)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        advance(hb, sb)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms64c = e0.elapsed_time(e1)
+        core.lib().lpm_bve_rk4_destroy(ha)
+        core.lib().lpm_bve_rk4_destroy(hb)
+        step_err = {"velocity_vertices": rel_errors(sa.vu, sb.vu),
+                    "velocity_leaf_faces": rel_errors(sa.fu, sb.fu, base.fm),
+                    "position_leaf_faces": rel_errors(sa.fx, sb.fx, base.fm),
+                    "vorticity_leaf_faces": rel_errors(sa.fz, sb.fz, base.fm)}
+
+        # ---- e2e: host buffers through the C ABI, copies inside the timing ----
+        hostbufs = {k: getattr(base, k).cpu().pin_memory() for k in ("vx", "vz", "vu", "fx", "fz", "fu")}
+        se = base.clone()
+        he = make_stepper(ctx, se, core.FP32C, flags)
+        h2d = d2h = 0
+        for name in hostbufs:
+            h2d += hostbufs[name].numel() * 8
+        d2h = h2d
+        advance(he, se)
+        torch.cuda.synchronize(device)
+        e2e_ms = 0.0
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for name, hb in hostbufs.items():
+                getattr(se, name).copy_(hb, non_blocking=True)
+            advance(he, se)
+            for name, hb in hostbufs.items():
+                hb.copy_(getattr(se, name), non_blocking=True)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            e2e_ms += a.elapsed_time(b)
+        core.lib().lpm_bve_rk4_destroy(he)
+        e2e_value = 4 * ipe * args.steps / (e2e_ms * 1e-3) / 1e9
+
+        cpu = cpu_baseline(host, args) if not args.no_cpu else None
+
+        result = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (generated icosahedral mesh + Gaussian vortex; no dataset)",
+            "config": workload_config(args.level, nv, nleaf),
+            "clocks": clocks,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp32", "achieved": round(achieved, 3),
+                         "peak": round(peak_fp32, 3), "unit": "TFLOP/s",
+                         "frac": round(achieved / peak_fp32, 4), "traffic": traffic,
+                         "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz "
+                                      "(sm_max_mhz of MEASURED_PEAKS.json)",
+                         "kernel": "nbody_f32<3,u> (sphere velocity, FP32 pairs, compensated)",
+                         "kernel_ms": round(nbody_ms, 4),
+                         "flops_per_pair_credited": FLOPS_PER_PAIR,
+                         "measured_fma_tflops": {"fp32": round(fma32, 2), "fp64": round(fma64, 3)},
+                         "frac_of_measured_fp32_fma": round(achieved / fma32, 4)},
+            "fp64": {"value": round(ipe / (ms64_eval * 1e-3) / 1e9, 4), "unit": UNIT,
+                     "ms_per_evaluation": round(ms64_eval, 2),
+                     "note": "one velocity evaluation (vertices + leaf faces) of the initial "
+                             "state, every pair term in the reference's FP64 arithmetic"},
+            "fp64_chord": {"value": round(4 * ipe / (ms64c * 1e-3) / 1e9, 4), "unit": UNIT,
+                           "ms_per_step": round(ms64c, 2),
+                           "note": "one RK4 step of the FP32C algorithm carried out in FP64"},
+            "errors_fp32c_vs_fp64": {
+                "one_evaluation_vs_reference_fp64": {"velocity_vertices": e_v,
+                                                     "velocity_leaf_faces": e_f},
+                "one_rk4_step_vs_fp64_chord": step_err},
+            "cpu_baseline": cpu,
+        }
+    return result
+
+
+def cpu_baseline(host, args):
+    """FP64 oracle (CPU restatement of the reference functors) on a bounded
+    target sample: n_sample vertex targets against all face slots."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import lpm_oracle
+
+    vx, fx, fa, fm, vz, fz = host
+    threads = os.cpu_count() or 1
+    lpm_oracle.set_threads(threads)
+    nleaf = int((fm == 0).sum())
+    n_sample = args.cpu_targets
+    idx = np.random.default_rng(20261203).choice(vx.shape[0], n_sample, replace=False)
+    idx.sort()
+    lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx[:256])  # warm
+    t0 = time.perf_counter()
+    lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx)
+    dt = time.perf_counter() - t0
+    pairs = n_sample * nleaf
+    return {"value": round(pairs / dt / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n_sample} seeded vertex targets x {nleaf} leaf sources, one FP64 velocity "
+                      f"evaluation ({dt:.1f} s)"}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the reference's CPU algorithm (FP64 port; the Kokkos build is
+# not buildable here), on this workload, all host threads
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import lpm_oracle
+
+    host = make_state(args.level)
+    vx, fx, fa, fm, vz, fz = host
+    nv, nleaf = vx.shape[0], int((fm == 0).sum())
+    threads = os.cpu_count() or 1
+    lpm_oracle.set_threads(threads)
+    n_sample = args.cpu_targets
+    rng = np.random.default_rng(20261203)
+    idx = np.sort(rng.choice(vx.shape[0], n_sample, replace=False))
+    for _ in range(max(args.warmup, 0)):
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx[:512])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx)
+    dt = time.perf_counter() - t0
+    value = args.steps * n_sample * nleaf / dt / 1e9
+    sample = (f"each step: one FP64 velocity evaluation of {n_sample} seeded vertex targets x "
+              f"{nleaf} leaf sources (a bounded sample of the RK4 step)")
+    return {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic", "config": workload_config(args.level, nv, nleaf),
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's Kokkos-OpenMP build cannot be compiled (Kokkos, "
+                    "KokkosKernels, MPI, spdlog, Catch2 absent); this is the FP64 CPU "
+                    "restatement of its functors in oracle/"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--level", type=int, default=LEVEL)
+    ap.add_argument("--cpu-targets", type=int, default=8192)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    res = run_ours(args, rank, world, local)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -51,6 +51,12 @@ extern "C" {
  *            per-tile Kahan/TwoSum-compensated sums, FP64 epilogue. */
 #define LPM_FP64 64
 #define LPM_FP32C 32
+/* LPM_FP64_CHORD: the LPM_FP32C algorithm (chord denominator, cross product
+ * hoisted out of the sum) in FP64.  On unit vectors it equals LPM_FP64 to
+ * rounding; off the sphere (RK stage positions, which leave the sphere by
+ * O(dt^2 |u|^2)) it keeps evaluating the sphere kernel, where the reference's
+ * 1 - x.y + eps^2 can turn non-positive. */
+#define LPM_FP64_CHORD 65
 
 /* geometry */
 #define LPM_PLANE 2
@@ -166,6 +172,9 @@ int lpm_err_norms(lpm_context* ctx, int ndim, int64_t n, lpm_view appx,
 #define LPM_STEP_SKIP_SELF_ALWAYS 8u /* ic2d: skip i == j also for eps > 0 */
 #define LPM_STEP_NO_GRAPH 16u     /* launch stages directly instead of
                                      replaying a captured CUDA graph */
+#define LPM_STEP_TIME_NBODY 32u   /* bracket every N-body launch with CUDA
+                                     events (implies LPM_STEP_NO_GRAPH); read
+                                     with lpm_*_nbody_time */
 
 typedef struct lpm_bve_rk4 lpm_bve_rk4;
 /* BVERK4(dt, sphere) + BVERK4::init (src/lpm_bve_rk4.hpp:10-77,
@@ -186,6 +195,10 @@ int lpm_bve_rk4_advance_timestep(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
                                  lpm_view fvel, const double* farea,
                                  const uint8_t* fmask);
 
+/* With LPM_STEP_TIME_NBODY: total device time (ms) and number of the N-body
+ * launches since the previous call (then reset).  Synchronous. */
+int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches);
+
 typedef struct lpm_ic2d_rk2 lpm_ic2d_rk2;
 /* Incompressible2DRK2(dt, ic2d) (src/lpm_incompressible2d_rk2_impl.hpp:15-43).
  * ndim = LPM_SPHERE or LPM_PLANE; cor = Coriolis Omega or beta. */
@@ -201,6 +214,7 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
                                   lpm_view fx, double* fzeta, lpm_view fvel,
                                   double* fpsi, const double* farea,
                                   const uint8_t* fmask);
+int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches);
 
 /* ---- host-side inputs: meshes and initial conditions -------------------- */
 /* Mesh kinds (restatements of the reference seeds' tree_init,

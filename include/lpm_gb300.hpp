@@ -1,0 +1,132 @@
+// lpm_gb300.hpp -- header-only C++17 facade over the C ABI (lpm_gb300.h) with
+// the reference's class and method names.
+//
+// A reference build swaps its Kokkos launches for these calls (see
+// INTEGRATION.md).  The facade needs no Kokkos: any view type with .data()
+// and .stride(0)/.stride(1) (Kokkos::View<Real*[3]> in either layout, or the
+// small DeviceArray below) converts to an lpm_view.  Nonzero status codes
+// become std::runtime_error, as LPM_REQUIRE does (src/lpm_assert.hpp:22-30).
+#ifndef LPM_GB300_HPP
+#define LPM_GB300_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+#include "lpm_gb300.h"
+
+namespace lpm_gb300 {
+
+inline void require(int rc, const char* what) {
+  if (rc != LPM_OK)
+    throw std::runtime_error(std::string(what) + ": " + lpm_last_error() +
+                             " (status " + std::to_string(rc) + ")");
+}
+
+// Strided view of an n x ndim array from any view-like object.
+template <typename V>
+lpm_view as_view(const V& v) {
+  return lpm_view{const_cast<double*>(reinterpret_cast<const double*>(v.data())),
+                  static_cast<int64_t>(v.stride(0)), static_cast<int64_t>(v.stride(1))};
+}
+inline lpm_view as_view(double* p, int64_t stride_i, int64_t stride_c) {
+  return lpm_view{p, stride_i, stride_c};
+}
+
+// Owns an lpm_context (device binding, stream, cached scratch).
+class Context {
+ public:
+  explicit Context(int device = 0, int precision = LPM_FP64) {
+    require(lpm_context_create(&h_, device), "lpm_context_create");
+    require(lpm_context_set_precision(h_, precision), "lpm_context_set_precision");
+  }
+  ~Context() { lpm_context_destroy(h_); }
+  Context(const Context&) = delete;
+  Context& operator=(const Context&) = delete;
+  lpm_context* get() const { return h_; }
+  void set_stream(void* s) { require(lpm_context_set_stream(h_, s), "set_stream"); }
+  void set_precision(int p) { require(lpm_context_set_precision(h_, p), "set_precision"); }
+  void synchronize() { require(lpm_context_synchronize(h_), "synchronize"); }
+
+ private:
+  lpm_context* h_ = nullptr;
+};
+
+// ---- functor-equivalent calls (src/lpm_bve_sphere_kernels.hpp) ------------
+inline void BVEVertexVelocity(Context& c, lpm_view u, lpm_view vx, int64_t nv, lpm_view fx,
+                              const double* zeta, const double* area,
+                              const uint8_t* mask, int64_t nf) {
+  require(lpm_bve_vertex_velocity(c.get(), u, vx, nv, fx, zeta, area, mask, nf),
+          "BVEVertexVelocity");
+}
+inline void BVEFaceVelocity(Context& c, lpm_view u, lpm_view fx, const double* zeta,
+                            const double* area, const uint8_t* mask, int64_t nf) {
+  require(lpm_bve_face_velocity(c.get(), u, fx, zeta, area, mask, nf), "BVEFaceVelocity");
+}
+inline void BVEVertexStreamFn(Context& c, double* psi, lpm_view vx, int64_t nv, lpm_view fx,
+                              const double* zeta, const double* area,
+                              const uint8_t* mask, int64_t nf) {
+  require(lpm_bve_vertex_stream_fn(c.get(), psi, vx, nv, fx, zeta, area, mask, nf),
+          "BVEVertexStreamFn");
+}
+inline void BVEFaceStreamFn(Context& c, double* psi, lpm_view fx, const double* zeta,
+                            const double* area, const uint8_t* mask, int64_t nf) {
+  require(lpm_bve_face_stream_fn(c.get(), psi, fx, zeta, area, mask, nf), "BVEFaceStreamFn");
+}
+
+// ---- BVERK4 (src/lpm_bve_rk4.hpp:10-77) ----------------------------------
+class BVERK4 {
+ public:
+  BVERK4(Context& c, double dt, int64_t nverts, int64_t nfaces, double Omega,
+         double eps = 0.0, int precision = LPM_FP64, uint32_t flags = 0)
+      : dt(dt), Omega(Omega) {
+    require(lpm_bve_rk4_create(c.get(), &h_, nverts, nfaces, dt, Omega, eps, precision, flags),
+            "BVERK4");
+  }
+  ~BVERK4() { lpm_bve_rk4_destroy(h_); }
+  BVERK4(const BVERK4&) = delete;
+  BVERK4& operator=(const BVERK4&) = delete;
+  void advance_timestep(lpm_view vx, double* vzeta, lpm_view vvel, lpm_view fx, double* fzeta,
+                        lpm_view fvel, const double* farea, const uint8_t* fmask) {
+    require(lpm_bve_rk4_advance_timestep(h_, vx, vzeta, vvel, fx, fzeta, fvel, farea, fmask),
+            "BVERK4::advance_timestep");
+  }
+  double dt, Omega;
+
+ private:
+  lpm_bve_rk4* h_ = nullptr;
+};
+
+// ---- Incompressible2DRK2 (src/lpm_incompressible2d_rk2.hpp) --------------
+class Incompressible2DRK2 {
+ public:
+  Incompressible2DRK2(Context& c, int ndim, double dt, int64_t n_passive, int64_t n_active,
+                      double eps, double coriolis, int precision = LPM_FP64,
+                      uint32_t flags = 0)
+      : dt(dt), eps(eps) {
+    require(lpm_ic2d_rk2_create(c.get(), &h_, ndim, n_passive, n_active, dt, eps, coriolis,
+                                precision, flags),
+            "Incompressible2DRK2");
+  }
+  ~Incompressible2DRK2() { lpm_ic2d_rk2_destroy(h_); }
+  Incompressible2DRK2(const Incompressible2DRK2&) = delete;
+  Incompressible2DRK2& operator=(const Incompressible2DRK2&) = delete;
+  void advance_timestep_impl(lpm_view vx, double* vzeta, lpm_view vvel, double* vpsi,
+                             lpm_view fx, double* fzeta, lpm_view fvel, double* fpsi,
+                             const double* farea, const uint8_t* fmask) {
+    require(lpm_ic2d_rk2_advance_timestep(h_, vx, vzeta, vvel, vpsi, fx, fzeta, fvel, fpsi,
+                                          farea, fmask),
+            "Incompressible2DRK2::advance_timestep_impl");
+    ++t_idx;
+  }
+  double dt, eps;
+  int t_idx = 0;
+
+ private:
+  lpm_ic2d_rk2* h_ = nullptr;
+};
+
+}  // namespace lpm_gb300
+
+#endif  // LPM_GB300_HPP

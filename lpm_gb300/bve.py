@@ -115,6 +115,13 @@ class BVERK4:
             ptr(sph.face_area), ptr(sph.face_mask)))
         sph.t += self.dt
 
+    def nbody_time(self) -> tuple[float, int]:
+        """(ms, launches) of the N-body kernels timed since the last call
+        (requires core.STEP_TIME_NBODY)."""
+        ms, n = C.c_double(), C.c_int64()
+        check(lib().lpm_bve_rk4_nbody_time(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def close(self) -> None:
         if self._h:
             lib().lpm_bve_rk4_destroy(self._h)

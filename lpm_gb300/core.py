@@ -22,6 +22,7 @@ LPM_ERR_STATE = -5
 
 FP64 = 64
 FP32C = 32
+FP64_CHORD = 65
 PLANE = 2
 SPHERE = 3
 
@@ -30,6 +31,7 @@ STEP_REPROJECT = 2
 STEP_SKIP_MASKED_TARGETS = 4
 STEP_SKIP_SELF_ALWAYS = 8
 STEP_NO_GRAPH = 16
+STEP_TIME_NBODY = 32
 
 MESH_ICOS_TRI = 1
 MESH_CUBED_SPHERE = 2
@@ -53,6 +55,7 @@ EXPORTS = [
     "lpm_bve_rk4_create", "lpm_bve_rk4_destroy", "lpm_bve_rk4_advance_timestep",
     "lpm_ic2d_rk2_create", "lpm_ic2d_rk2_destroy", "lpm_ic2d_rk2_advance_timestep",
     "lpm_mesh_sizes", "lpm_mesh_build", "lpm_ic_eval", "lpm_measure_fma_peak",
+    "lpm_bve_rk4_nbody_time", "lpm_ic2d_rk2_nbody_time",
 ]
 
 
@@ -118,6 +121,8 @@ def _declare(L: C.CDLL) -> None:
         "lpm_mesh_build": [i32, i32, dbl, vp, vp, vp, vp],
         "lpm_ic_eval": [i32, vp, i32, i32, i64, vp, vp],
         "lpm_measure_fma_peak": [vp, i32, C.POINTER(dbl)],
+        "lpm_bve_rk4_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
+        "lpm_ic2d_rk2_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -204,8 +204,9 @@ int lpm_context_set_stream(lpm_context* ctx, void* stream) {
 
 int lpm_context_set_precision(lpm_context* ctx, int precision) {
   if (!ctx) return fail(LPM_ERR_ARG, "null context");
-  if (precision != LPM_FP64 && precision != LPM_FP32C)
-    return fail(LPM_ERR_ARG, "precision must be LPM_FP64 (64) or LPM_FP32C (32)");
+  if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
+    return fail(LPM_ERR_ARG,
+                "precision must be LPM_FP64 (64), LPM_FP64_CHORD (65) or LPM_FP32C (32)");
   ctx->precision = precision;
   return LPM_OK;
 }

@@ -2,6 +2,7 @@
 // small O(N) device utilities behind the functor entry points.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <cstring>
 #include <vector>
 
@@ -96,9 +97,9 @@ __global__ void k_scatter_map(const uint8_t* mask, int64_t n, const int* boff,
   }
 }
 
-// Packed sources.  FP32: (x, y, z, zeta*area); FP64: (x, y, z, g) with
-// g = (-zeta)*area for the BVE form, zeta*area otherwise.
-template <bool F32>
+// Packed sources.  Chord modes: (x, y, z, zeta*area); FP64 reference mode:
+// (x, y, z, g) with g = (-zeta)*area for the BVE form, zeta*area otherwise.
+template <int MODE>
 __global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
                            View x, int ndim, const double* zeta,
                            const double* area, int form, void* out) {
@@ -110,9 +111,9 @@ __global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
     p0 = x(s, 0);
     p1 = x(s, 1);
     if (ndim == 3) p2 = x(s, 2);
-    g = (form == FORM_BVE && !F32) ? (-zeta[s]) * area[s] : zeta[s] * area[s];
+    g = (form == FORM_BVE && MODE == M_REF64) ? (-zeta[s]) * area[s] : zeta[s] * area[s];
   }
-  if (F32) {
+  if (MODE == M_C32) {
     reinterpret_cast<float4*>(out)[k] = make_float4(
         __double2float_rn(p0), __double2float_rn(p1), __double2float_rn(p2),
         __double2float_rn(g));
@@ -121,9 +122,10 @@ __global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
   }
 }
 
-// Packed targets of one segment at offset off.  FP32: w = g of the skipped
-// self source (for the psi self-term correction), else 0.  FP64: tself.
-template <bool F32>
+// Packed targets of one segment at offset off.  Chord modes: w = g of the
+// skipped self source (for the psi self-term correction), else 0.  FP64
+// reference mode: tself = skipped source index or -1.
+template <int MODE>
 __global__ void k_pack_tgt(int64_t off, int64_t n, View x, int ndim,
                            const int* slot2src, bool skip_self,
                            const double* zeta, const double* area, void* out,
@@ -133,12 +135,13 @@ __global__ void k_pack_tgt(int64_t off, int64_t n, View x, int ndim,
   const double p0 = x(i, 0), p1 = x(i, 1), p2 = ndim == 3 ? x(i, 2) : 0.0;
   int self = -1;
   if (skip_self && slot2src) self = slot2src[i];
-  if (F32) {
-    float gs = 0.f;
-    if (self >= 0) gs = __double2float_rn(zeta[i] * area[i]);
+  const double gs = self >= 0 ? zeta[i] * area[i] : 0.0;
+  if (MODE == M_C32) {
     reinterpret_cast<float4*>(out)[off + i] =
         make_float4(__double2float_rn(p0), __double2float_rn(p1),
-                    __double2float_rn(p2), gs);
+                    __double2float_rn(p2), __double2float_rn(gs));
+  } else if (MODE == M_C64) {
+    reinterpret_cast<double4*>(out)[off + i] = make_double4(p0, p1, p2, gs);
   } else {
     reinterpret_cast<double4*>(out)[off + i] = make_double4(p0, p1, p2, 0.0);
     tself[off + i] = self;
@@ -157,13 +160,14 @@ __global__ void k_fill_pad_tgt(int64_t from, int64_t to, bool f32, void* out,
   }
 }
 
-// Deterministic sum of the packed FP32 source strengths (two passes).
-__global__ void k_sum_g_partial(const float4* src, int64_t n, double* part) {
+// Deterministic sum of the packed source strengths (two passes).
+__global__ void k_sum_g_partial(const void* src, bool f32, int64_t n, double* part) {
   __shared__ double sh[256];
   double s = 0;
   for (int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * 256)
-    s += (double)src[k].w;
+    s += f32 ? (double)static_cast<const float4*>(src)[k].w
+             : static_cast<const double4*>(src)[k].w;
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
@@ -181,11 +185,11 @@ __global__ void k_sum_final(const double* part, int n, double* out) {
 }
 
 // Combine the chunk partials of one segment and write its outputs.
-template <bool F32, int NDIM, bool WU, bool WP>
+template <int MODE, int NDIM, bool WU, bool WP>
 __global__ void k_combine(const double* __restrict__ part, int nchunks,
                           int64_t ntgt_pad, int64_t off, int64_t n, View x,
-                          View u, double* psi, const float4* tgt32,
-                          const double* sg, float c0) {
+                          View u, double* psi, const void* tgt,
+                          const double* sg, double c0) {
   constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -198,65 +202,57 @@ __global__ void k_combine(const double* __restrict__ part, int nchunks,
 #pragma unroll
     for (int k = 0; k < NC; ++k) a[k] += p[k * ntgt_pad];
   }
-  if (!F32) {
+  if (MODE == M_REF64) {
     if (WU)
 #pragma unroll
       for (int k = 0; k < NDIM; ++k) u(i, k) = a[k];
     if (WP) psi[i] = a[NC - 1];
     return;
   }
-  constexpr double INV2PI = 1.0 / (2.0 * kPI);
-  constexpr double LN2_4PI = 0.69314718055994530942 / (4.0 * kPI);
-  if (WU) {
-    if (NDIM == 3) {
-      const double x0 = x(i, 0), x1 = x(i, 1), x2 = x(i, 2);
-      u(i, 0) = -INV2PI * (a[1] * x2 - a[2] * x1);
-      u(i, 1) = -INV2PI * (a[2] * x0 - a[0] * x2);
-      u(i, 2) = -INV2PI * (a[0] * x1 - a[1] * x0);
-    } else {
-      u(i, 0) = -INV2PI * a[1];
-      u(i, 1) = INV2PI * a[0];
-    }
-  }
-  if (WP) {
-    const float gs = tgt32[t].w;
-    double L = a[NC - 1] - (double)gs * (double)lg2_approx(c0);
-    if (NDIM == 3) L -= (*sg - (double)gs);
-    psi[i] = -LN2_4PI * L;
-  }
+  double pos[3] = {x(i, 0), x(i, 1), NDIM == 3 ? x(i, 2) : 0.0};
+  double uu[3], ps = 0;
+  const double gs = MODE == M_C32 ? (double)static_cast<const float4*>(tgt)[t].w
+                                  : static_cast<const double4*>(tgt)[t].w;
+  chord_epilogue<MODE, NDIM, WU, WP>(a, pos, gs, sg, c0, uu, &ps);
+  if (WU)
+#pragma unroll
+    for (int k = 0; k < NDIM; ++k) u(i, k) = uu[k];
+  if (WP) psi[i] = ps;
 }
 
-template <bool F32, int NDIM, bool WU, bool WP>
+template <int MODE, int NDIM, bool WU, bool WP>
 void launch_combine(lpm_context& ctx, const NbodyPlan& p, const double* part,
-                    int64_t off, const TgtSeg& seg, const float4* tgt32,
-                    const double* sg, float c0) {
+                    int64_t off, const TgtSeg& seg, const void* tgt,
+                    const double* sg, double c0) {
   const int th = 256;
   const int64_t nb = (seg.n + th - 1) / th;
-  k_combine<F32, NDIM, WU, WP><<<nb, th, 0, ctx.stream>>>(
-      part, p.nchunks, p.ntgt_pad, off, seg.n, seg.x, seg.u, seg.psi, tgt32,
-      sg, c0);
+  k_combine<MODE, NDIM, WU, WP><<<nb, th, 0, ctx.stream>>>(
+      part, p.nchunks, p.ntgt_pad, off, seg.n, seg.x, seg.u, seg.psi, tgt, sg, c0);
   ctx.launches++;
 }
 
-template <bool F32, int NDIM>
+template <int MODE, int NDIM>
 void combine_dispatch(lpm_context& ctx, const NbodyPlan& p, const double* part,
-                      int64_t off, const TgtSeg& seg, const float4* tgt32,
-                      const double* sg, float c0) {
+                      int64_t off, const TgtSeg& seg, const void* tgt,
+                      const double* sg, double c0) {
   if (p.wu && p.wp)
-    launch_combine<F32, NDIM, true, true>(ctx, p, part, off, seg, tgt32, sg, c0);
+    launch_combine<MODE, NDIM, true, true>(ctx, p, part, off, seg, tgt, sg, c0);
   else if (p.wu)
-    launch_combine<F32, NDIM, true, false>(ctx, p, part, off, seg, tgt32, sg, c0);
+    launch_combine<MODE, NDIM, true, false>(ctx, p, part, off, seg, tgt, sg, c0);
   else
-    launch_combine<F32, NDIM, false, true>(ctx, p, part, off, seg, tgt32, sg, c0);
+    launch_combine<MODE, NDIM, false, true>(ctx, p, part, off, seg, tgt, sg, c0);
 }
 
-template <int NDIM, bool WU, bool WP>
-void launch_f32(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
-                const void* src, double* part, float c0) {
-  dim3 grid(unsigned(p.ntgt_pad / (F32_NT * F32_R)), unsigned(p.nchunks));
-  nbody_f32<NDIM, WU, WP, F32_R, F32_NT, F32_TILE><<<grid, F32_NT, 0, ctx.stream>>>(
-      static_cast<const float4*>(tgt), static_cast<const float4*>(src),
-      p.ntgt_pad, p.nsrc_pad, p.chunk_len, c0, part, ctx.d_err);
+template <typename T, int NDIM, bool WU, bool WP>
+void launch_chord(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                  const void* src, double* part, T c0) {
+  constexpr bool F = std::is_same<T, float>::value;
+  constexpr int NT = F ? F32_NT : F64_NT, R = F ? F32_R : F64_R, TILE = F ? F32_TILE : F64_TILE;
+  using V4 = typename Vec4<T>::type;
+  dim3 grid(unsigned(p.ntgt_pad / (NT * R)), unsigned(p.nchunks));
+  nbody_chord<T, NDIM, WU, WP, R, NT, TILE><<<grid, NT, 0, ctx.stream>>>(
+      static_cast<const V4*>(tgt), static_cast<const V4*>(src), p.ntgt_pad, p.nsrc_pad,
+      p.chunk_len, c0, part, ctx.d_err);
   ctx.launches++;
 }
 
@@ -281,25 +277,29 @@ void f64_want(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
     launch_f64<FORM, false, true>(ctx, p, tgt, tself, src, part, eps2);
 }
 
-template <int NDIM>
-void f32_want(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
-              const void* src, double* part, float c0) {
+template <typename T, int NDIM>
+void chord_want(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                const void* src, double* part, T c0) {
   if (p.wu && p.wp)
-    launch_f32<NDIM, true, true>(ctx, p, tgt, src, part, c0);
+    launch_chord<T, NDIM, true, true>(ctx, p, tgt, src, part, c0);
   else if (p.wu)
-    launch_f32<NDIM, true, false>(ctx, p, tgt, src, part, c0);
+    launch_chord<T, NDIM, true, false>(ctx, p, tgt, src, part, c0);
   else
-    launch_f32<NDIM, false, true>(ctx, p, tgt, src, part, c0);
+    launch_chord<T, NDIM, false, true>(ctx, p, tgt, src, part, c0);
 }
 
 int occupancy(int precision) {
-  static int occ32 = 0, occ64 = 0;
-  int& o = precision == LPM_FP32C ? occ32 : occ64;
+  static int occ[3] = {0, 0, 0};
+  const int m = mode_of(precision);
+  int& o = occ[m];
   if (o == 0) {
     int v = 0;
-    if (precision == LPM_FP32C)
+    if (m == M_C32)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_f32<3, true, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
+          &v, nbody_chord<float, 3, true, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
+    else if (m == M_C64)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &v, nbody_chord<double, 3, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &v, nbody_f64<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
@@ -310,9 +310,11 @@ int occupancy(int precision) {
 
 }  // namespace
 
-float f32_c0(int ndim, double eps) {
+float f32_c0(int ndim, double eps) { return float(chord_c0(ndim, eps)); }
+
+double chord_c0(int ndim, double eps) {
   const double e2 = eps * eps;
-  return float((ndim == 3 ? 2.0 * e2 : e2) + 1e-30);
+  return (ndim == 3 ? 2.0 * e2 : e2) + 1e-30;
 }
 
 int64_t compact_sources(lpm_context& ctx, const uint8_t* mask, int64_t nslots,
@@ -366,12 +368,19 @@ NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
 void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
                   const int* tself, const void* src, double* part,
                   double eps) {
-  if (p.precision == LPM_FP32C) {
+  const int m = mode_of(p.precision);
+  if (m == M_C32) {
     const float c0 = f32_c0(p.ndim, eps);
     if (p.ndim == 3)
-      f32_want<3>(ctx, p, tgt, src, part, c0);
+      chord_want<float, 3>(ctx, p, tgt, src, part, c0);
     else
-      f32_want<2>(ctx, p, tgt, src, part, c0);
+      chord_want<float, 2>(ctx, p, tgt, src, part, c0);
+  } else if (m == M_C64) {
+    const double c0 = chord_c0(p.ndim, eps);
+    if (p.ndim == 3)
+      chord_want<double, 3>(ctx, p, tgt, src, part, c0);
+    else
+      chord_want<double, 2>(ctx, p, tgt, src, part, c0);
   } else {
     const double eps2 = eps * eps;
     if (p.form == FORM_BVE)
@@ -384,23 +393,80 @@ void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
   LPM_CUDA(cudaGetLastError());
 }
 
+void sum_strengths(lpm_context& ctx, const void* src, bool f32, int64_t nsrc,
+                   double* out, double* scratch256) {
+  k_sum_g_partial<<<256, 256, 0, ctx.stream>>>(src, f32, nsrc, scratch256);
+  k_sum_final<<<1, 32, 0, ctx.stream>>>(scratch256, 256, out);
+  ctx.launches += 2;
+}
+
+namespace {
+template <int MODE>
+void pack_and_launch(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
+                     const TgtSeg* segs, int nseg, int64_t ntgt, const NbodyPlan& p,
+                     const int* slot2src, const int* src2slot, void* srcp, void* tgtp,
+                     int* tself, double* part, double* sgp) {
+  const int th = 256;
+  const int ndim = spec.ndim;
+  k_pack_src<MODE><<<(p.nsrc_pad + th - 1) / th, th, 0, ctx.stream>>>(
+      src2slot, p.nsrc, p.nsrc_pad, src.x, ndim, src.zeta, src.area, spec.form, srcp);
+  ctx.launches++;
+  int64_t off = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const TgtSeg& g = segs[s];
+    if (g.n > 0) {
+      const int* map = g.collocated ? slot2src : nullptr;
+      const bool skip = g.collocated && spec.skip_self;
+      k_pack_tgt<MODE><<<(g.n + th - 1) / th, th, 0, ctx.stream>>>(
+          off, g.n, g.x, ndim, map, skip, src.zeta, src.area, tgtp, tself);
+      ctx.launches++;
+    }
+    off += g.n;
+  }
+  if (p.ntgt_pad > ntgt) {
+    k_fill_pad_tgt<<<(p.ntgt_pad - ntgt + th - 1) / th, th, 0, ctx.stream>>>(
+        ntgt, p.ntgt_pad, MODE == M_C32, tgtp, tself);
+    ctx.launches++;
+  }
+  if (MODE != M_REF64 && spec.want_psi && ndim == 3)
+    sum_strengths(ctx, srcp, MODE == M_C32, p.nsrc, sgp, sgp + 8);
+  LPM_CUDA(cudaGetLastError());
+
+  launch_nbody(ctx, p, tgtp, tself, srcp, part, spec.eps);
+
+  const double c0 = MODE == M_C32 ? double(f32_c0(ndim, spec.eps)) : chord_c0(ndim, spec.eps);
+  off = 0;
+  for (int s = 0; s < nseg; ++s) {
+    const TgtSeg& g = segs[s];
+    if (g.n > 0) {
+      if (ndim == 3)
+        combine_dispatch<MODE, 3>(ctx, p, part, off, g, tgtp, sgp, c0);
+      else
+        combine_dispatch<MODE, 2>(ctx, p, part, off, g, tgtp, sgp, c0);
+    }
+    off += g.n;
+  }
+  LPM_CUDA(cudaGetLastError());
+}
+}  // namespace
+
 void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
                 const TgtSeg* segs, int nseg) {
   int64_t ntgt = 0;
   for (int s = 0; s < nseg; ++s) ntgt += segs[s].n;
   if (ntgt == 0) return;
-  const bool f32 = spec.precision == LPM_FP32C;
+  const int m = mode_of(spec.precision);
   const int ndim = spec.ndim;
 
   ctx.arena.reset();
   // Upper bounds first, so one reservation covers the whole call.
   NbodyPlan p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
                            spec.want_psi, ntgt, src.nslots);
-  const size_t rec = f32 ? sizeof(float4) : sizeof(double4);
+  const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4);
   const size_t need = 4096 + sizeof(int) * (2 * size_t(src.nslots) + 2 * (size_t(src.nslots) / SCAN_BLOCK + 2)) +
                       rec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
                       sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes() +
-                      sizeof(double) * 1200 + 8 * 256;
+                      sizeof(double) * 300 + 8 * 256;
   ctx.arena.reserve(need);
 
   int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(1, src.nslots)));
@@ -413,72 +479,16 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   void* tgtp = ctx.arena.take(rec * size_t(p.ntgt_pad));
   int* tself = static_cast<int*>(ctx.arena.take(sizeof(int) * size_t(p.ntgt_pad)));
   double* part = static_cast<double*>(ctx.arena.take(p.part_bytes()));
-  double* sgp = static_cast<double*>(ctx.arena.take(sizeof(double) * 1040));
-
-  const int th = 256;
-  {
-    const int64_t nb = (p.nsrc_pad + th - 1) / th;
-    if (f32)
-      k_pack_src<true><<<nb, th, 0, ctx.stream>>>(src2slot, nsrc, p.nsrc_pad, src.x, ndim,
-                                                  src.zeta, src.area, spec.form, srcp);
-    else
-      k_pack_src<false><<<nb, th, 0, ctx.stream>>>(src2slot, nsrc, p.nsrc_pad, src.x, ndim,
-                                                   src.zeta, src.area, spec.form, srcp);
-    ctx.launches++;
-  }
-  int64_t off = 0;
-  for (int s = 0; s < nseg; ++s) {
-    const TgtSeg& g = segs[s];
-    if (g.n > 0) {
-      const int64_t nb = (g.n + th - 1) / th;
-      const int* map = g.collocated ? slot2src : nullptr;
-      const bool skip = g.collocated && spec.skip_self;
-      if (f32)
-        k_pack_tgt<true><<<nb, th, 0, ctx.stream>>>(off, g.n, g.x, ndim, map, skip,
-                                                    src.zeta, src.area, tgtp, tself);
-      else
-        k_pack_tgt<false><<<nb, th, 0, ctx.stream>>>(off, g.n, g.x, ndim, map, skip,
-                                                     src.zeta, src.area, tgtp, tself);
-      ctx.launches++;
-    }
-    off += g.n;
-  }
-  if (p.ntgt_pad > ntgt) {
-    const int64_t nb = (p.ntgt_pad - ntgt + th - 1) / th;
-    k_fill_pad_tgt<<<nb, th, 0, ctx.stream>>>(ntgt, p.ntgt_pad, f32, tgtp, tself);
-    ctx.launches++;
-  }
-  if (f32 && spec.want_psi && ndim == 3) {
-    k_sum_g_partial<<<1024, 256, 0, ctx.stream>>>(static_cast<const float4*>(srcp), nsrc,
-                                                  sgp + 8);
-    k_sum_final<<<1, 32, 0, ctx.stream>>>(sgp + 8, 1024, sgp);
-    ctx.launches += 2;
-  }
-  LPM_CUDA(cudaGetLastError());
-
-  launch_nbody(ctx, p, tgtp, tself, srcp, part, spec.eps);
-
-  const float c0 = f32_c0(ndim, spec.eps);
-  off = 0;
-  for (int s = 0; s < nseg; ++s) {
-    const TgtSeg& g = segs[s];
-    if (g.n > 0) {
-      const float4* t32 = static_cast<const float4*>(tgtp);
-      if (f32) {
-        if (ndim == 3)
-          combine_dispatch<true, 3>(ctx, p, part, off, g, t32, sgp, c0);
-        else
-          combine_dispatch<true, 2>(ctx, p, part, off, g, t32, sgp, c0);
-      } else {
-        if (ndim == 3)
-          combine_dispatch<false, 3>(ctx, p, part, off, g, t32, sgp, c0);
-        else
-          combine_dispatch<false, 2>(ctx, p, part, off, g, t32, sgp, c0);
-      }
-    }
-    off += g.n;
-  }
-  LPM_CUDA(cudaGetLastError());
+  double* sgp = static_cast<double*>(ctx.arena.take(sizeof(double) * 264));
+  if (m == M_C32)
+    pack_and_launch<M_C32>(ctx, spec, src, segs, nseg, ntgt, p, slot2src, src2slot, srcp,
+                           tgtp, tself, part, sgp);
+  else if (m == M_C64)
+    pack_and_launch<M_C64>(ctx, spec, src, segs, nseg, ntgt, p, slot2src, src2slot, srcp,
+                           tgtp, tself, part, sgp);
+  else
+    pack_and_launch<M_REF64>(ctx, spec, src, segs, nseg, ntgt, p, slot2src, src2slot, srcp,
+                             tgtp, tself, part, sgp);
 }
 
 // ---------------------------------------------------------------------------

@@ -150,6 +150,11 @@ void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
 // FP32 squared-distance offset c0 (2 eps^2 on the sphere, eps^2 on the plane,
 // plus the 1e-30 floor).
 float f32_c0(int ndim, double eps);
+double chord_c0(int ndim, double eps);
+// Deterministic sum of the .w strengths of nsrc packed source records into
+// *out (scratch256: 256 doubles).
+void sum_strengths(lpm_context& ctx, const void* src, bool f32, int64_t nsrc,
+                   double* out, double* scratch256);
 
 // Small device utilities (direct_sum.cu).
 void bve_tendency(lpm_context& ctx, double* dzeta, View u, int64_t n,

@@ -29,7 +29,11 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
+
 #include <cuda_runtime.h>
+
+#include "lpm_gb300.h"
 
 namespace lpm {
 
@@ -163,19 +167,40 @@ struct TilePipe {
 };
 
 // ---------------------------------------------------------------------------
-// FP32 compensated kernel.
-//   tgt: float4 (x, y, z, unused) per target, ntgt_pad entries
-//   src: float4 (x, y, z, g) per source (plane: z = 0), nsrc_pad entries
+// Chord-form kernel, FP32 (LPM_FP32C) or FP64 (LPM_FP64_CHORD).
+//   tgt: vec4 (x, y, z, g_self) per target, ntgt_pad entries
+//   src: vec4 (x, y, z, g) per source (plane: z = 0), nsrc_pad entries
 //   part: [chunk][comp][ntgt_pad] doubles; comps = (WU ? NDIM : 0) +
 //         (WP ? 1 : 0): (w0 w1 [w2] [L]) with L = sum g lg2 q
+// FP32 uses the MUFU reciprocal and log2; FP64 divides and calls log2.
 // ---------------------------------------------------------------------------
-template <int NDIM, bool WU, bool WP, int R, int NT, int TILE>
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
+__device__ __forceinline__ float chord_rcp(float q) { return rcp_approx(q); }
+__device__ __forceinline__ double chord_rcp(double q) { return 1.0 / q; }
+__device__ __forceinline__ float chord_lg2(float q) { return lg2_approx(q); }
+__device__ __forceinline__ double chord_lg2(double q) { return log2(q); }
+__device__ __forceinline__ float chord_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double chord_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ void two_sum_acc(double& s, double& c, double p) {
+  const double t = s + p;
+  const double bp = t - s;
+  const double e = (s - (t - bp)) + (p - bp);
+  s = t;
+  c += e;
+}
+
+template <typename T, int NDIM, bool WU, bool WP, int R, int NT, int TILE>
 __global__ void __launch_bounds__(NT)
-    nbody_f32(const float4* __restrict__ tgt, const float4* __restrict__ src,
-              int64_t ntgt_pad, int64_t nsrc_pad, int chunk_len, float c0,
-              double* __restrict__ part, int* err) {
+    nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
+                const typename Vec4<T>::type* __restrict__ src, int64_t ntgt_pad,
+                int64_t nsrc_pad, int chunk_len, T c0, double* __restrict__ part,
+                int* err) {
+  using V4 = typename Vec4<T>::type;
   constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
-  __shared__ __align__(128) float4 sbuf[2 * TILE];
+  __shared__ __align__(128) V4 sbuf[2 * TILE];
   __shared__ __align__(8) uint64_t sbar[2];
 
   const int tid = threadIdx.x;
@@ -184,60 +209,60 @@ __global__ void __launch_bounds__(NT)
   int64_t slen = nsrc_pad - s0;
   if (slen > chunk_len) slen = chunk_len;
 
-  float tx[R], ty[R], tz[R];
+  T tx[R], ty[R], tz[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const float4 t = tgt[tbase + r * NT + tid];
+    const V4 t = tgt[tbase + r * NT + tid];
     tx[r] = t.x;
     ty[r] = t.y;
     tz[r] = t.z;
   }
-  float S[NC][R], C[NC][R];
+  T S[NC][R], C[NC][R];
 #pragma unroll
   for (int k = 0; k < NC; ++k)
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      S[k][r] = 0.f;
-      C[k][r] = 0.f;
+      S[k][r] = T(0);
+      C[k][r] = T(0);
     }
 
-  TilePipe<float4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  TilePipe<V4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
   pipe.start();
   for (int t = 0; t < pipe.ntiles; ++t) {
     if (!pipe.acquire(t)) {
       pipe.drain(t, err);
       return;
     }
-    const float4* sm = pipe.tile(t);
-    float P[NC][R];
+    const V4* sm = pipe.tile(t);
+    T P[NC][R];
 #pragma unroll
     for (int k = 0; k < NC; ++k)
 #pragma unroll
-      for (int r = 0; r < R; ++r) P[k][r] = 0.f;
+      for (int r = 0; r < R; ++r) P[k][r] = T(0);
 
 #pragma unroll 4
     for (int j = 0; j < TILE; ++j) {
-      const float4 s = sm[j];
+      const V4 s = sm[j];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const float dx = tx[r] - s.x;
-        const float dy = ty[r] - s.y;
-        float q;
-        float dz = 0.f;
+        const T dx = tx[r] - s.x;
+        const T dy = ty[r] - s.y;
+        T q;
+        T dz = T(0);
         if (NDIM == 3) {
           dz = tz[r] - s.z;
-          q = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, c0)));
+          q = chord_fma(dx, dx, chord_fma(dy, dy, chord_fma(dz, dz, c0)));
         } else {
-          q = fmaf(dx, dx, fmaf(dy, dy, c0));
+          q = chord_fma(dx, dx, chord_fma(dy, dy, c0));
         }
         if (WU) {
-          const float w = s.w * rcp_approx(q);
-          P[0][r] = fmaf(w, dx, P[0][r]);
-          P[1][r] = fmaf(w, dy, P[1][r]);
-          if (NDIM == 3) P[2][r] = fmaf(w, dz, P[2][r]);
+          const T w = s.w * chord_rcp(q);
+          P[0][r] = chord_fma(w, dx, P[0][r]);
+          P[1][r] = chord_fma(w, dy, P[1][r]);
+          if (NDIM == 3) P[2][r] = chord_fma(w, dz, P[2][r]);
         }
         if (WP) {
-          P[NC - 1][r] = fmaf(s.w, lg2_approx(q), P[NC - 1][r]);
+          P[NC - 1][r] = chord_fma(s.w, chord_lg2(q), P[NC - 1][r]);
         }
       }
     }
@@ -390,8 +415,47 @@ __global__ void __launch_bounds__(NT)
     for (int r = 0; r < R; ++r) out[k * ntgt_pad + tbase + r * NT + tid] = A[k][r];
 }
 
+// Arithmetic modes of the pair sum.
+enum Mode : int {
+  M_REF64 = 0,  // LPM_FP64: the reference's formulas, FP64
+  M_C32 = 1,    // LPM_FP32C: chord form, FP32 pairs, compensated sums
+  M_C64 = 2     // LPM_FP64_CHORD: chord form, FP64
+};
+__host__ __device__ inline int mode_of(int precision) {
+  return precision == LPM_FP32C ? M_C32 : (precision == LPM_FP64_CHORD ? M_C64 : M_REF64);
+}
+
+// Chord-form epilogue of one target: a = summed partials (w [, L]), p = the
+// FP64 position the target was evaluated at, gs = strength of its skipped
+// self source (0 if none), sg = sum of all source strengths (sphere psi).
+template <int MODE, int NDIM, bool WU, bool WP>
+__device__ __forceinline__ void chord_epilogue(const double* a, const double* p,
+                                               double gs, const double* sg,
+                                               double c0, double* u, double* psi) {
+  constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
+  constexpr double INV2PI = 1.0 / (2.0 * kPI);
+  constexpr double LN2_4PI = 0.69314718055994530942 / (4.0 * kPI);
+  if (WU) {
+    if (NDIM == 3) {
+      u[0] = -INV2PI * (a[1] * p[2] - a[2] * p[1]);
+      u[1] = -INV2PI * (a[2] * p[0] - a[0] * p[2]);
+      u[2] = -INV2PI * (a[0] * p[1] - a[1] * p[0]);
+    } else {
+      u[0] = -INV2PI * a[1];
+      u[1] = INV2PI * a[0];
+    }
+  }
+  if (WP) {
+    // remove the self pair the kernel added (d = 0, q = c0)
+    const double lgc = MODE == M_C32 ? (double)lg2_approx((float)c0) : log2(c0);
+    double L = a[NC - 1] - gs * lgc;
+    if (NDIM == 3) L -= (*sg - gs);
+    *psi = -LN2_4PI * L;
+  }
+}
+
 // Launch shapes.  FP32: 256 threads x 4 targets, 512-source tiles (8 KB per
-// buffer).  FP64: 128 threads x 2 targets, 256-source tiles (8 KB).
+// buffer).  FP64 (both forms): 128 threads x 2 targets, 256-source tiles.
 constexpr int F32_NT = 256, F32_R = 4, F32_TILE = 512;
 constexpr int F64_NT = 128, F64_R = 2, F64_TILE = 256;
 

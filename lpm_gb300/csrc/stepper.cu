@@ -59,7 +59,7 @@ struct Tg {
 
 // Packed tiles and partials of the stepper's evaluations.
 struct Pk {
-  bool f32;
+  int mode;  // M_REF64, M_C32 or M_C64
   int form;
   bool skip_self;
   void* tgt;
@@ -68,7 +68,6 @@ struct Pk {
   const double* part;
   int nchunks;
   int64_t tpad;
-  const float* sg;  // unused placeholder for alignment
 };
 
 // Pack target t (and its source record when it is an unmasked face) at
@@ -83,16 +82,20 @@ __device__ void pack(const Tg& g, const Pk& k, int64_t t, const double* p,
     area = g.farea[s];
   }
   const double p2 = g.ndim == 3 ? p[2] : 0.0;
-  if (k.f32) {
+  const bool self = k.skip_self && src >= 0;
+  if (k.mode == M_C32) {
     const float gw = src >= 0 ? __double2float_rn(dm(z, area)) : 0.f;
     const float4 r = make_float4(__double2float_rn(p[0]), __double2float_rn(p[1]),
                                  __double2float_rn(p2), gw);
-    static_cast<float4*>(k.tgt)[t] =
-        make_float4(r.x, r.y, r.z, (k.skip_self && src >= 0) ? gw : 0.f);
+    static_cast<float4*>(k.tgt)[t] = make_float4(r.x, r.y, r.z, self ? gw : 0.f);
     if (src >= 0) static_cast<float4*>(k.src)[src] = r;
+  } else if (k.mode == M_C64) {
+    const double gw = src >= 0 ? dm(z, area) : 0.0;
+    static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, self ? gw : 0.0);
+    if (src >= 0) static_cast<double4*>(k.src)[src] = make_double4(p[0], p[1], p2, gw);
   } else {
     static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, 0.0);
-    k.tself[t] = (k.skip_self && src >= 0) ? src : -1;
+    k.tself[t] = self ? src : -1;
     if (src >= 0) {
       const double gg = (k.form == FORM_BVE) ? dm(-z, area) : dm(z, area);
       static_cast<double4*>(k.src)[src] = make_double4(p[0], p[1], p2, gg);
@@ -100,38 +103,47 @@ __device__ void pack(const Tg& g, const Pk& k, int64_t t, const double* p,
   }
 }
 
-// Sum of the chunk partials of target t.  FP32: converts w into u (and the
+// Sum of the chunk partials of target t; chord modes turn w into u (and the
 // log sum into psi) with the FP64 position p at which t was evaluated.
-__device__ void combine(const Tg& g, const Pk& k, int64_t t, const double* p,
-                        bool wp, float c0, const double* sg, double* u,
-                        double* psi) {
-  const int nd = g.ndim;
-  const int nc = nd + (wp ? 1 : 0);
-  double a[4] = {0, 0, 0, 0};
+template <int NDIM, bool WP>
+__device__ void combine_t(const Pk& k, int64_t t, const double* p, double c0,
+                          const double* sg, double* u, double* psi) {
+  constexpr int NC = NDIM + (WP ? 1 : 0);
+  double a[NC];
+#pragma unroll
+  for (int m = 0; m < NC; ++m) a[m] = 0.0;
   for (int c = 0; c < k.nchunks; ++c) {
-    const double* q = k.part + (int64_t)c * nc * k.tpad + t;
-    for (int m = 0; m < nc; ++m) a[m] += q[m * k.tpad];
+    const double* q = k.part + (int64_t)c * NC * k.tpad + t;
+#pragma unroll
+    for (int m = 0; m < NC; ++m) a[m] += q[m * k.tpad];
   }
-  if (!k.f32) {
-    for (int m = 0; m < nd; ++m) u[m] = a[m];
-    if (wp) *psi = a[nd];
+  if (k.mode == M_REF64) {
+    for (int m = 0; m < NDIM; ++m) u[m] = a[m];
+    if (WP) *psi = a[NDIM];
     return;
   }
-  constexpr double INV2PI = 1.0 / (2.0 * kPI);
-  constexpr double LN2_4PI = 0.69314718055994530942 / (4.0 * kPI);
-  if (nd == 3) {
-    u[0] = -INV2PI * (a[1] * p[2] - a[2] * p[1]);
-    u[1] = -INV2PI * (a[2] * p[0] - a[0] * p[2]);
-    u[2] = -INV2PI * (a[0] * p[1] - a[1] * p[0]);
+  if (k.mode == M_C32) {
+    const double gs = (double)static_cast<const float4*>(k.tgt)[t].w;
+    chord_epilogue<M_C32, NDIM, true, WP>(a, p, gs, sg, c0, u, psi);
   } else {
-    u[0] = -INV2PI * a[1];
-    u[1] = INV2PI * a[0];
+    const double gs = static_cast<const double4*>(k.tgt)[t].w;
+    chord_epilogue<M_C64, NDIM, true, WP>(a, p, gs, sg, c0, u, psi);
   }
-  if (wp) {
-    const float gs = static_cast<const float4*>(k.tgt)[t].w;
-    double L = a[nd] - (double)gs * (double)lg2_approx(c0);
-    if (nd == 3) L -= (*sg - (double)gs);
-    *psi = -LN2_4PI * L;
+}
+
+__device__ void combine(const Tg& g, const Pk& k, int64_t t, const double* p,
+                        bool wp, double c0, const double* sg, double* u,
+                        double* psi) {
+  if (g.ndim == 3) {
+    if (wp)
+      combine_t<3, true>(k, t, p, c0, sg, u, psi);
+    else
+      combine_t<3, false>(k, t, p, c0, sg, u, psi);
+  } else {
+    if (wp)
+      combine_t<2, true>(k, t, p, c0, sg, u, psi);
+    else
+      combine_t<2, false>(k, t, p, c0, sg, u, psi);
   }
 }
 
@@ -147,7 +159,7 @@ struct Rk4Buf {
 struct Rk4Par {
   double dt, Omega;
   bool fix_facevort3, reproject;
-  float c0;
+  double c0;
 };
 
 __device__ __forceinline__ double bve_tend(double uz, double dt, double Om) {
@@ -241,7 +253,7 @@ struct Rk2Buf {
 };
 struct Rk2Par {
   double dt, cor;
-  float c0;
+  double c0;
   const double* sg;  // device: sum of source strengths (FP32 sphere psi)
 };
 
@@ -319,29 +331,6 @@ __global__ void k_face_targets(const uint8_t* mask, int64_t nf, bool skip,
   }
 }
 
-// Deterministic sum of packed FP32 source strengths into *out.
-__global__ void k_sg_partial(const float4* src, int64_t n, double* part) {
-  __shared__ double sh[256];
-  double s = 0;
-  for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * 256)
-    s += (double)src[i].w;
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
-__global__ void k_sg_final(const double* part, int n, double* out) {
-  if (threadIdx.x == 0) {
-    double s = 0;
-    for (int i = 0; i < n; ++i) s += part[i];
-    *out = s;
-  }
-}
-
 }  // namespace
 }  // namespace lpm
 
@@ -380,6 +369,8 @@ struct lpm_stepper_base {
     return p;
   }
   void free_all() {
+    for (cudaEvent_t e : timers) cudaEventDestroy(e);
+    timers.clear();
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
     if (cap_stream) cudaStreamDestroy(cap_stream);
@@ -406,7 +397,7 @@ struct lpm_stepper_base {
       c.launches++;
     }
     plan = lpm::plan_nbody(c, precision, ndim, form, true, want_psi, T, nsrc);
-    const size_t rec = precision == LPM_FP32C ? 16 : 32;
+    const size_t rec = precision == LPM_FP32C ? 16 : 32;  // float4 / double4
     tgt = dalloc(rec * plan.ntgt_pad);
     src = dalloc(rec * plan.nsrc_pad);
     tself = static_cast<int*>(dalloc(sizeof(int) * plan.ntgt_pad));
@@ -445,9 +436,12 @@ struct lpm_stepper_base {
     g.farea = farea;
     return g;
   }
+  double c0() const {
+    return precision == LPM_FP32C ? double(lpm::f32_c0(ndim, eps)) : lpm::chord_c0(ndim, eps);
+  }
   lpm::Pk packs() const {
     lpm::Pk k;
-    k.f32 = precision == LPM_FP32C;
+    k.mode = lpm::mode_of(precision);
     k.form = form;
     k.skip_self = skip_self;
     k.tgt = tgt;
@@ -456,24 +450,46 @@ struct lpm_stepper_base {
     k.part = part;
     k.nchunks = plan.nchunks;
     k.tpad = plan.ntgt_pad;
-    k.sg = nullptr;
     return k;
   }
   void nbody() {
-    if (precision == LPM_FP32C && want_psi && ndim == 3) {
-      lpm::k_sg_partial<<<256, 256, 0, ctx->stream>>>(static_cast<const float4*>(src),
-                                                      nsrc, sgbuf + 8);
-      lpm::k_sg_final<<<1, 32, 0, ctx->stream>>>(sgbuf + 8, 256, sgbuf);
-      ctx->launches += 2;
+    if (precision != LPM_FP64 && want_psi && ndim == 3)
+      lpm::sum_strengths(*ctx, src, precision == LPM_FP32C, nsrc, sgbuf, sgbuf + 8);
+    if (flags & LPM_STEP_TIME_NBODY) {
+      cudaEvent_t e[2];
+      LPM_CUDA(cudaEventCreate(&e[0]));
+      LPM_CUDA(cudaEventCreate(&e[1]));
+      LPM_CUDA(cudaEventRecord(e[0], ctx->stream));
+      lpm::launch_nbody(*ctx, plan, tgt, tself, src, part, eps);
+      LPM_CUDA(cudaEventRecord(e[1], ctx->stream));
+      timers.push_back(e[0]);
+      timers.push_back(e[1]);
+      return;
     }
     lpm::launch_nbody(*ctx, plan, tgt, tself, src, part, eps);
+  }
+
+  std::vector<cudaEvent_t> timers;
+  // Sums and clears the recorded N-body timings.
+  void nbody_time(double* ms, int64_t* n) {
+    LPM_CUDA(cudaStreamSynchronize(ctx->stream));
+    double tot = 0;
+    for (size_t i = 0; i + 1 < timers.size(); i += 2) {
+      float m = 0;
+      LPM_CUDA(cudaEventElapsedTime(&m, timers[i], timers[i + 1]));
+      tot += m;
+    }
+    *ms = tot;
+    *n = int64_t(timers.size() / 2);
+    for (cudaEvent_t e : timers) cudaEventDestroy(e);
+    timers.clear();
   }
 
   // Runs `body` either directly or through a graph captured for this key.
   template <typename F>
   void run(const std::vector<char>& k, F body) {
     lpm_context& c = *ctx;
-    if (flags & LPM_STEP_NO_GRAPH) {
+    if (flags & (LPM_STEP_NO_GRAPH | LPM_STEP_TIME_NBODY)) {
       body();
       LPM_CUDA(cudaGetLastError());
       return;
@@ -537,7 +553,7 @@ struct lpm_bve_rk4 : lpm_stepper_base {
     P.Omega = Omega;
     P.fix_facevort3 = flags & LPM_STEP_FIX_FACEVORT3;
     P.reproject = flags & LPM_STEP_REPROJECT;
-    P.c0 = lpm::f32_c0(3, eps);
+    P.c0 = c0();
 
     std::vector<char> kk(sizeof(lpm::Tg));
     std::memcpy(kk.data(), &g, sizeof(g));
@@ -578,7 +594,7 @@ struct lpm_ic2d_rk2 : lpm_stepper_base {
     lpm::Rk2Par P;
     P.dt = dt;
     P.cor = cor;
-    P.c0 = lpm::f32_c0(ndim, eps);
+    P.c0 = c0();
     P.sg = sgbuf;
     std::vector<char> kk(sizeof(lpm::Tg));
     std::memcpy(kk.data(), &g, sizeof(g));
@@ -614,8 +630,9 @@ int lpm_bve_rk4_create(lpm_context* ctx, lpm_bve_rk4** out, int64_t nverts,
     if (!ctx || !out) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: null argument");
     if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
       return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: sizes out of range");
-    if (precision != LPM_FP64 && precision != LPM_FP32C)
-      return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: precision must be LPM_FP64 or LPM_FP32C");
+    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
+      return lpm::fail(LPM_ERR_ARG,
+                       "lpm_bve_rk4_create: precision must be LPM_FP64, LPM_FP64_CHORD or LPM_FP32C");
     if (!std::isfinite(dt) || !std::isfinite(Omega) || !std::isfinite(eps) || eps < 0)
       return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: non-finite dt/Omega or bad eps");
     auto* st = new lpm_bve_rk4();
@@ -671,7 +688,7 @@ int lpm_ic2d_rk2_create(lpm_context* ctx, lpm_ic2d_rk2** out, int ndim,
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: ndim must be 2 or 3");
     if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: sizes out of range");
-    if (precision != LPM_FP64 && precision != LPM_FP32C)
+    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: bad precision");
     if (!std::isfinite(dt) || !std::isfinite(cor) || !std::isfinite(eps) || eps < 0)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: non-finite dt/cor or bad eps");
@@ -716,6 +733,28 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_advance_timestep: null array");
     cudaSetDevice(st->ctx->device);
     st->advance(vx, vzeta, vvel, vpsi, fx, fzeta, fvel, fpsi, farea, fmask);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches) {
+  try {
+    if (!st || !ms || !launches) return lpm::fail(LPM_ERR_ARG, "null argument");
+    cudaSetDevice(st->ctx->device);
+    st->nbody_time(ms, launches);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches) {
+  try {
+    if (!st || !ms || !launches) return lpm::fail(LPM_ERR_ARG, "null argument");
+    cudaSetDevice(st->ctx->device);
+    st->nbody_time(ms, launches);
     return LPM_OK;
   } catch (...) {
     return lpm::handle_exception();

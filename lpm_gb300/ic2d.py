@@ -125,6 +125,11 @@ class Incompressible2DRK2:
             ptr(s.face_mask)))
         self.t_idx += 1
 
+    def nbody_time(self) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_int64()
+        check(lib().lpm_ic2d_rk2_nbody_time(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def close(self) -> None:
         if self._h:
             lib().lpm_ic2d_rk2_destroy(self._h)

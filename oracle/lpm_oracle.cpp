@@ -73,18 +73,32 @@ inline void scross(double* c, const double* a, const double* b) {
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+// Sphere-kernel form.  0 = the reference's 1 - x.y; 1 = the chord form
+// |x - y|^2 / 2, equal to 1 - x.y for unit vectors and free of its
+// cancellation; it keeps evaluating the sphere kernel at RK stage positions,
+// which leave the unit sphere.  The chord form is not the reference's
+// arithmetic: it is the oracle for the LPM_FP64_CHORD / LPM_FP32C paths.
+int g_chord = 0;
+
+// 1 - x.y, or the chord form
+inline double one_minus_dot(const double* x, const double* y) {
+  if (!g_chord) return 1 - sdot(x, y);
+  const double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+  return 0.5 * (d0 * d0 + d1 * d1 + d2 * d2);
+}
+
 // greens_fn, src/lpm_sphere_functions.hpp:21-29.
 inline double greens_fn(const double* tgt, const double* src, double vort,
                         double area) {
   const double circ = -vort * area;
-  return std::log(1 - sdot(tgt, src)) * circ / (4 * PI);
+  return std::log(one_minus_dot(tgt, src)) * circ / (4 * PI);
 }
 
 // biot_savart, src/lpm_sphere_functions.hpp:44-57.
 inline void biot_savart(double* u, const double* tgt, const double* src,
                         double vort, double area) {
   scross(u, tgt, src);
-  const double strength = -vort * area / (4 * PI * (1 - sdot(src, tgt)));
+  const double strength = -vort * area / (4 * PI * one_minus_dot(src, tgt));
   for (int j = 0; j < 3; ++j) u[j] *= strength;
 }
 
@@ -92,7 +106,7 @@ inline void biot_savart(double* u, const double* tgt, const double* src,
 // src/lpm_incompressible2d_kernels.hpp:35-47.
 inline void sphere_kernel_vals(double* r, const double* x, const double* y,
                                double eps) {
-  const double arg = 1 - sdot(x, y) + eps * eps;
+  const double arg = one_minus_dot(x, y) + eps * eps;
   scross(r, x, y);
   for (int k = 0; k < 3; ++k) r[k] /= (-4 * PI * arg);
   r[3] = -std::log(arg) / (4 * PI);
@@ -196,6 +210,9 @@ extern "C" {
 int oracle_version(void) { return 1; }
 
 void oracle_set_threads(int n) { g_threads = n; }
+
+// 0: the reference's sphere arithmetic (default); 1: chord form.
+void oracle_set_sphere_form(int chord) { g_chord = chord ? 1 : 0; }
 
 int oracle_max_threads(void) {
 #ifdef _OPENMP

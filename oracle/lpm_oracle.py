@@ -34,6 +34,7 @@ def lib() -> C.CDLL:
         vp, l, i, d = C.c_void_p, C.c_long, C.c_int, C.c_double
         sig = {
             "oracle_set_threads": [i],
+            "oracle_set_sphere_form": [i],
             "oracle_max_threads": [],
             "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
             "oracle_bve_face_solve": [vp, vp, l, vp, vp, vp, vp, vp, l, i],
@@ -64,6 +65,23 @@ def _f(a, shape=None):
 
 def set_threads(n: int) -> None:
     lib().oracle_set_threads(int(n))
+
+
+def set_sphere_form(chord: bool) -> None:
+    """False: the reference's 1 - x.y (default); True: the chord form."""
+    lib().oracle_set_sphere_form(int(bool(chord)))
+
+
+class chord_form:
+    """Context manager evaluating sphere kernels in the chord form."""
+
+    def __enter__(self):
+        set_sphere_form(True)
+        return self
+
+    def __exit__(self, *exc):
+        set_sphere_form(False)
+        return False
 
 
 def max_threads() -> int:

@@ -17,15 +17,32 @@ from lpm_gb300 import functors as F
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
+TOL64C = 1e-11  # FP64 chord form vs the chord-form oracle (different operation order)
 TOL32 = 2e-6
 OMEGA = 2 * math.pi
 
 
 def rel(a, b):
+    """max|a-b| / max|b| over finite entries; the non-finite entries must match.
+
+    The reference's FP64 arithmetic divides by zero at a divided parent slot
+    whose centre coincides with its central child's centre (1 - x.y == 0), so
+    both the oracle and the FP64 path give inf/nan there."""
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
+    fa, fb = np.isfinite(a), np.isfinite(b)
+    assert np.array_equal(fa, fb), "non-finite entries differ"
+    a, b = a[fb], b[fb]
+    if b.size == 0:
+        return 0.0
     den = np.abs(b).max()
     return np.abs(a - b).max() / (den if den > 0 else 1.0)
+
+
+def same(a, b):
+    """Bitwise-equal finite values and the same non-finite pattern."""
+    fa, fb = torch.isfinite(a), torch.isfinite(b)
+    return torch.equal(fa, fb) and torch.equal(a[fa], b[fb])
 
 
 def dev(a):
@@ -43,14 +60,22 @@ def sphere_case(level, seed=core.MESH_ICOS_TRI, kind=core.IC_RH54, params=None, 
     return vx, fx, fa, fm, zf
 
 
+def tolerance(precision):
+    return {core.FP64: TOL64, core.FP64_CHORD: TOL64C, core.FP32C: TOL32}[precision]
+
+
 @pytest.mark.parametrize("level", [0, 2, 3])
-@pytest.mark.parametrize("precision", [core.FP64, core.FP32C])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP64_CHORD, core.FP32C])
 def test_bve_functors(gpu_ctx, oracle, level, precision):
     ctx = gpu_ctx
     ctx.set_precision(precision)
     vx, fx, fa, fm, zf = sphere_case(level, noise=0.5)
-    psi_v, u_v = oracle.bve_vertex_solve(vx, fx, zf, fa, fm)
-    psi_f, u_f = oracle.bve_face_solve(fx, zf, fa, fm)
+    oracle.set_sphere_form(precision != core.FP64)
+    try:
+        psi_v, u_v = oracle.bve_vertex_solve(vx, fx, zf, fa, fm)
+        psi_f, u_f = oracle.bve_face_solve(fx, zf, fa, fm)
+    finally:
+        oracle.set_sphere_form(False)
     dvx, dfx, dz, da, dm = dev(vx), dev(fx), dev(zf), dev(fa), dev(fm)
     gu = torch.zeros(vx.shape[0], 3, dtype=torch.float64, device="cuda")
     gp = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
@@ -66,10 +91,11 @@ def test_bve_functors(gpu_ctx, oracle, level, precision):
         assert rel(gfu.cpu(), u_f) < TOL64
         assert rel(gfp.cpu(), psi_f) < TOL64
     else:
-        assert rel(gu.cpu(), u_v) < TOL32
-        assert rel(gp.cpu(), psi_v) < TOL32
-        assert rel(gfu.cpu().numpy()[leaf], u_f[leaf]) < TOL32
-        assert rel(gfp.cpu().numpy()[leaf], psi_f[leaf]) < TOL32
+        tol = tolerance(precision)
+        assert rel(gu.cpu(), u_v) < tol
+        assert rel(gp.cpu(), psi_v) < tol
+        assert rel(gfu.cpu().numpy()[leaf], u_f[leaf]) < tol
+        assert rel(gfp.cpu().numpy()[leaf], psi_f[leaf]) < tol
     # velocity-only and stream-function-only launches give the same values
     gu2 = torch.zeros_like(gu)
     F.bve_vertex_velocity(ctx, gu2, dvx, dfx, dz, da, dm)
@@ -80,7 +106,7 @@ def test_bve_functors(gpu_ctx, oracle, level, precision):
     gfp2 = torch.zeros_like(gfp)
     F.bve_face_stream_fn(ctx, gfp2, dfx, dz, da, dm)
     ctx.synchronize()
-    assert torch.equal(gu2, gu) and torch.equal(gfu2, gfu)
+    assert same(gu2, gu) and same(gfu2, gfu)
     tolp = 0 if precision == core.FP64 else 1e-12
     assert rel(gp2.cpu(), gp.cpu()) <= tolp and rel(gfp2.cpu(), gfp.cpu()) <= tolp
 
@@ -106,7 +132,7 @@ def test_bve_soa_layout(gpu_ctx, oracle):
 
 
 @pytest.mark.parametrize("eps", [0.0, 0.05])
-@pytest.mark.parametrize("precision", [core.FP64, core.FP32C])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP64_CHORD, core.FP32C])
 @pytest.mark.parametrize("geom", ["sphere", "plane"])
 def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
     ctx = gpu_ctx
@@ -119,8 +145,12 @@ def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
         vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 4, 4.0)
         zf = core.eval_ic(core.IC_DIPOLE_PAIR, (2.0, 1.0, -2.0, 0.0, -2.0, 1.0, 2.0, 0.0), fx)
     nd = vx.shape[1]
-    u_p, psi_p = oracle.ic2d_passive_sums(vx, fx, zf, fa, fm, eps)
-    u_a, psi_a = oracle.ic2d_active_sums(fx, zf, fa, fm, eps)
+    oracle.set_sphere_form(precision != core.FP64)
+    try:
+        u_p, psi_p = oracle.ic2d_passive_sums(vx, fx, zf, fa, fm, eps)
+        u_a, psi_a = oracle.ic2d_active_sums(fx, zf, fa, fm, eps)
+    finally:
+        oracle.set_sphere_form(False)
     gu = torch.zeros(vx.shape[0], nd, dtype=torch.float64, device="cuda")
     gp = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
     fu = torch.zeros(fx.shape[0], nd, dtype=torch.float64, device="cuda")
@@ -130,7 +160,7 @@ def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
     F.ic2d_active_sums(ctx, fu, fp, dfx, dz, da, dm, eps)
     ctx.synchronize()
     leaf = fm == 0
-    tol = TOL64 if precision == core.FP64 else TOL32
+    tol = tolerance(precision)
     assert rel(gu.cpu(), u_p) < tol
     assert rel(gp.cpu(), psi_p) < tol
     sel = slice(None) if precision == core.FP64 else leaf
@@ -175,7 +205,7 @@ def test_determinism(gpu_ctx):
             F.bve_face_velocity(ctx, u, dev(fx), dev(zf), dev(fa), dev(fm))
             outs.append(u)
         ctx.synchronize()
-        assert torch.equal(outs[0], outs[1])
+        assert same(outs[0], outs[1])
 
 
 def test_argument_errors(gpu_ctx):
@@ -206,7 +236,12 @@ def test_tendencies_and_invariants(gpu_ctx, oracle):
     assert np.array_equal(dz.cpu().numpy(), -(2 * OMEGA * u[:, 2]))
     inv = F.ic2d_invariants(ctx, dev(zf), dev(u), dev(fa), dev(fm))
     ref = oracle.invariants(zf, u, fa, fm)
-    assert np.allclose(inv, ref, rtol=1e-12, atol=0)
+    # sums in a different order: compare against the sum of magnitudes
+    leaf = fm == 0
+    scale = [np.abs(zf * fa)[leaf].sum(), 0.5 * (zf * zf * fa)[leaf].sum(),
+             0.5 * ((u * u).sum(1) * fa)[leaf].sum()]
+    for a, b, s in zip(inv, ref, scale):
+        assert abs(a - b) <= 1e-13 * s
     en = F.err_norms(ctx, dev(u + 1e-3), dev(u), dev(fa), dev(fm))
     er = oracle.err_norms(u + 1e-3, u, fa, fm)
     assert np.allclose(en, er, rtol=1e-12)
