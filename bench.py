@@ -253,6 +253,14 @@ def run_ours(args, rank, world, device):
     core.lib().lpm_bve_rk4_destroy(h)
 
     result = {}
+    if args.only_headline:
+        if rank == 0:
+            result = {"metric": METRIC, "value": round(value, 3), "unit": UNIT,
+                      "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": round(ms_per_step, 4), "gpu_launches": launches,
+                      "config": workload_config(args.level, nv, nleaf),
+                      "note": "headline leg only (profiling run)"}
+        return result
     if rank == 0:
         # ---- kernel timing for the roofline (events around each N-body) ----
         st2 = base.clone()
@@ -449,6 +457,8 @@ def main():
     ap.add_argument("--level", type=int, default=LEVEL)
     ap.add_argument("--cpu-targets", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only-headline", action="store_true",
+                    help="time the FP32C steps only (for profiler runs)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

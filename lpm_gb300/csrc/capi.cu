@@ -42,6 +42,10 @@ int handle_exception() {
 
 void Arena::reserve(size_t bytes) {
   if (bytes <= cap) return;
+  if (fixed)
+    throw Error(LPM_ERR_ARG, "this call needs " + std::to_string(bytes) +
+                                 " bytes of scratch; the fixed scratch holds " +
+                                 std::to_string(cap));
   if (base) {
     cudaDeviceSynchronize();
     cudaFree(base);

@@ -243,17 +243,26 @@ void combine_dispatch(lpm_context& ctx, const NbodyPlan& p, const double* part,
     launch_combine<MODE, NDIM, false, true>(ctx, p, part, off, seg, tgt, sg, c0);
 }
 
-template <typename T, int NDIM, bool WU, bool WP>
-void launch_chord(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
-                  const void* src, double* part, T c0) {
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC>
+void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                    const void* src, double* part, T c0) {
   constexpr bool F = std::is_same<T, float>::value;
   constexpr int NT = F ? F32_NT : F64_NT, R = F ? F32_R : F64_R, TILE = F ? F32_TILE : F64_TILE;
   using V4 = typename Vec4<T>::type;
   dim3 grid(unsigned(p.ntgt_pad / (NT * R)), unsigned(p.nchunks));
-  nbody_chord<T, NDIM, WU, WP, R, NT, TILE><<<grid, NT, 0, ctx.stream>>>(
+  nbody_chord<T, NDIM, WU, WP, SKIPC, R, NT, TILE><<<grid, NT, 0, ctx.stream>>>(
       static_cast<const V4*>(tgt), static_cast<const V4*>(src), p.ntgt_pad, p.nsrc_pad,
       p.chunk_len, c0, part, ctx.d_err);
   ctx.launches++;
+}
+
+template <typename T, int NDIM, bool WU, bool WP>
+void launch_chord(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                  const void* src, double* part, T c0) {
+  if (WP && p.skipc)
+    launch_chord_k<T, NDIM, WU, WP, WP>(ctx, p, tgt, src, part, c0);
+  else
+    launch_chord_k<T, NDIM, WU, WP, false>(ctx, p, tgt, src, part, c0);
 }
 
 template <int FORM, bool WU, bool WP>
@@ -296,10 +305,10 @@ int occupancy(int precision) {
     int v = 0;
     if (m == M_C32)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_chord<float, 3, true, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
+          &v, nbody_chord<float, 3, true, false, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
     else if (m == M_C64)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_chord<double, 3, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
+          &v, nbody_chord<double, 3, true, false, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &v, nbody_f64<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
@@ -358,7 +367,14 @@ NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
   // Aim for ~16 waves of CTAs so the tail of the last wave stays small.
   const int64_t slots = int64_t(std::max(ctx.num_sms, 1)) * occupancy(precision);
   int64_t nch = (16 * slots + ntb - 1) / ntb;
+  if (ctx.max_part_bytes > 0) {
+    const int64_t per_chunk = int64_t(sizeof(double)) * p.ncomp * p.ntgt_pad;
+    nch = std::min<int64_t>(nch, int64_t(ctx.max_part_bytes) / per_chunk);
+  }
   nch = std::max<int64_t>(1, std::min<int64_t>(nch, ntiles));
+  // fewer sources never give more chunks than this (the rounding below can
+  // raise nchunks when ntiles shrinks, but never above nch)
+  p.nchunks_max = int(nch);
   const int64_t tiles_per_chunk = (ntiles + nch - 1) / nch;
   p.chunk_len = int(tiles_per_chunk * tile);
   p.nchunks = int((ntiles + tiles_per_chunk - 1) / tiles_per_chunk);
@@ -465,7 +481,7 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4);
   const size_t need = 4096 + sizeof(int) * (2 * size_t(src.nslots) + 2 * (size_t(src.nslots) / SCAN_BLOCK + 2)) +
                       rec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
-                      sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes() +
+                      sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes_max() +
                       sizeof(double) * 300 + 8 * 256;
   ctx.arena.reserve(need);
 
@@ -474,6 +490,8 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   const int64_t nsrc = compact_sources(ctx, src.mask, src.nslots, slot2src, src2slot);
   p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
                  spec.want_psi, ntgt, nsrc);
+  for (int s = 0; s < nseg; ++s)
+    if (segs[s].collocated && spec.skip_self) p.skipc = true;
 
   void* srcp = ctx.arena.take(rec * size_t(p.nsrc_pad));
   void* tgtp = ctx.arena.take(rec * size_t(p.ntgt_pad));

@@ -57,11 +57,13 @@ enum Form : int {
   FORM_PLANE = 2   // Incompressible2DKernels<PlaneGeometry>
 };
 
-// Grow-only device arena owned by a context.
+// Grow-only device arena owned by a context.  A fixed arena wraps memory it
+// does not own and never reallocates: reserve() beyond its capacity throws.
 struct Arena {
   char* base = nullptr;
   size_t cap = 0;
   size_t off = 0;
+  bool fixed = false;
   void reserve(size_t bytes);
   void reset() { off = 0; }
   void* take(size_t bytes) {
@@ -83,6 +85,7 @@ struct lpm_context {
   int* d_err = nullptr;  // device flag: nonzero after a bounded wait gave up
   lpm::Arena arena;
   int64_t launches = 0;
+  size_t max_part_bytes = 0;  // cap on chunk-partial scratch (0 = none)
 };
 
 namespace lpm {
@@ -136,8 +139,13 @@ struct NbodyPlan {
   int64_t nsrc, nsrc_pad;
   int nchunks;
   int chunk_len;
+  int nchunks_max;     // bound on nchunks for any nsrc <= this plan's nsrc
+  bool skipc = false;  // chord stream function: drop coincident (i == j) pairs
   size_t part_bytes() const {
     return sizeof(double) * size_t(ncomp) * size_t(nchunks) * size_t(ntgt_pad);
+  }
+  size_t part_bytes_max() const {
+    return sizeof(double) * size_t(ncomp) * size_t(nchunks_max) * size_t(ntgt_pad);
   }
 };
 NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,

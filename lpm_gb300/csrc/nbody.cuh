@@ -192,7 +192,9 @@ __device__ __forceinline__ void two_sum_acc(double& s, double& c, double p) {
   c += e;
 }
 
-template <typename T, int NDIM, bool WU, bool WP, int R, int NT, int TILE>
+// SKIPC: in the stream-function sum, drop coincident pairs (q == c0, i.e.
+// d == 0: the skipped i == j term).  The velocity term of such a pair is 0.
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE>
 __global__ void __launch_bounds__(NT)
     nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
                 const typename Vec4<T>::type* __restrict__ src, int64_t ntgt_pad,
@@ -262,7 +264,9 @@ __global__ void __launch_bounds__(NT)
           if (NDIM == 3) P[2][r] = chord_fma(w, dz, P[2][r]);
         }
         if (WP) {
-          P[NC - 1][r] = chord_fma(s.w, chord_lg2(q), P[NC - 1][r]);
+          T lg = chord_lg2(q);
+          if (SKIPC) lg = (q == c0) ? T(0) : lg;
+          P[NC - 1][r] = chord_fma(s.w, lg, P[NC - 1][r]);
         }
       }
     }
@@ -428,6 +432,7 @@ __host__ __device__ inline int mode_of(int precision) {
 // Chord-form epilogue of one target: a = summed partials (w [, L]), p = the
 // FP64 position the target was evaluated at, gs = strength of its skipped
 // self source (0 if none), sg = sum of all source strengths (sphere psi).
+// c0 is unused (kept for the signature of both modes).
 template <int MODE, int NDIM, bool WU, bool WP>
 __device__ __forceinline__ void chord_epilogue(const double* a, const double* p,
                                                double gs, const double* sg,
@@ -446,9 +451,9 @@ __device__ __forceinline__ void chord_epilogue(const double* a, const double* p,
     }
   }
   if (WP) {
-    // remove the self pair the kernel added (d = 0, q = c0)
-    const double lgc = MODE == M_C32 ? (double)lg2_approx((float)c0) : log2(c0);
-    double L = a[NC - 1] - gs * lgc;
+    // the kernel dropped the skipped self pair (d = 0); remove its strength
+    // from the sum of strengths
+    double L = a[NC - 1];
     if (NDIM == 3) L -= (*sg - gs);
     *psi = -LN2_4PI * L;
   }

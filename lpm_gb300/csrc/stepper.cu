@@ -397,6 +397,7 @@ struct lpm_stepper_base {
       c.launches++;
     }
     plan = lpm::plan_nbody(c, precision, ndim, form, true, want_psi, T, nsrc);
+    plan.skipc = skip_self;
     const size_t rec = precision == LPM_FP32C ? 16 : 32;  // float4 / double4
     tgt = dalloc(rec * plan.ntgt_pad);
     src = dalloc(rec * plan.nsrc_pad);

@@ -21,7 +21,9 @@ from lpm_gb300.ic2d import Incompressible2D, Incompressible2DRK2, colliding_dipo
 pytestmark = pytest.mark.gpu
 
 OMEGA = 2 * math.pi
-TOLS = {core.FP64: (1e-12, 1e-12), core.FP64_CHORD: (1e-11, 1e-12), core.FP32C: (2e-6, 1e-8)}
+# (velocity / stream function, positions); FP32C positions carry the ~1e-7
+# velocity error times dt |u| per step
+TOLS = {core.FP64: (1e-12, 1e-12), core.FP64_CHORD: (1e-11, 1e-12), core.FP32C: (2e-6, 1e-7)}
 
 
 def rel(a, b, sel=slice(None)):
