@@ -106,6 +106,18 @@ int lpm_bve_vertex_velocity(lpm_context* ctx, lpm_view u, lpm_view vx,
                             int64_t nverts, lpm_view fx, const double* zeta,
                             const double* area, const uint8_t* mask,
                             int64_t nfaces);
+/* No counterpart in the reference.  BVEVertexVelocity in LPM_FP32C for
+ * callers that cannot allocate device memory: it calls no cudaMalloc or
+ * cudaFree and needs no context.  Its scratch is one 64 MiB array inside the
+ * library, held on every GPU that loads it until the process exits; problems
+ * needing more (about 24 B per face slot + 40 B per target) are rejected with
+ * LPM_ERR_ARG.  The first call on a device looks up the array's address; make
+ * it before any stream capture.  Calls share the array: calls that overlap on
+ * the GPU race.  Runs on `cuda_stream` and returns after it has finished. */
+int lpm_bve_vertex_velocity_static(lpm_view u, lpm_view vx, int64_t nverts,
+                                   lpm_view fx, const double* zeta,
+                                   const double* area, const uint8_t* mask,
+                                   int64_t nfaces, void* cuda_stream);
 /* BVEFaceSolve (:284-320): collocated face targets, i == j skipped. */
 int lpm_bve_face_solve(lpm_context* ctx, double* psi, lpm_view u, lpm_view fx,
                        const double* zeta, const double* area,

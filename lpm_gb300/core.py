@@ -55,7 +55,7 @@ EXPORTS = [
     "lpm_bve_rk4_create", "lpm_bve_rk4_destroy", "lpm_bve_rk4_advance_timestep",
     "lpm_ic2d_rk2_create", "lpm_ic2d_rk2_destroy", "lpm_ic2d_rk2_advance_timestep",
     "lpm_mesh_sizes", "lpm_mesh_build", "lpm_ic_eval", "lpm_measure_fma_peak",
-    "lpm_bve_rk4_nbody_time", "lpm_ic2d_rk2_nbody_time",
+    "lpm_bve_rk4_nbody_time", "lpm_ic2d_rk2_nbody_time", "lpm_bve_vertex_velocity_static",
 ]
 
 
@@ -123,6 +123,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_measure_fma_peak": [vp, i32, C.POINTER(dbl)],
         "lpm_bve_rk4_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ic2d_rk2_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
+        "lpm_bve_vertex_velocity_static": [V, V, i64, V, vp, vp, vp, i64, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
