@@ -228,6 +228,38 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
                                   const uint8_t* fmask);
 int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches);
 
+/* ---- ensembles of independent BVE problems ----------------------------- */
+/* No single reference counterpart: many BVESphere/BVERK4 instances advanced
+ * together.  Problem p owns nverts[p] vertex rows and nfaces[p] face-slot
+ * rows of the concatenated arrays (problem 0 first).  fmask: device, all
+ * face slots (fixed).  precision: LPM_FP32C or LPM_FP64_CHORD (chord form,
+ * velocity only).  Each evaluation is one persistent launch over (problem,
+ * target block, source chunk) work items; a step is replayed from a CUDA
+ * graph; the chunk length is autotuned on the first call. */
+typedef struct lpm_ensemble lpm_ensemble;
+int lpm_ensemble_create(lpm_context* ctx, lpm_ensemble** out, int nproblems,
+                        const int64_t* nverts, const int64_t* nfaces,
+                        const uint8_t* fmask, double dt, double Omega,
+                        double eps, int precision, uint32_t flags);
+int lpm_ensemble_destroy(lpm_ensemble* e);
+/* Velocities of the current state of every problem (one evaluation). */
+int lpm_ensemble_velocity(lpm_ensemble* e, lpm_view vx, lpm_view vvel,
+                          lpm_view fx, const double* fzeta, lpm_view fvel,
+                          const double* farea);
+/* One RK4 step of every problem (BVERK4::advance_timestep semantics). */
+int lpm_ensemble_advance_timestep(lpm_ensemble* e, lpm_view vx, double* vzeta,
+                                  lpm_view vvel, lpm_view fx, double* fzeta,
+                                  lpm_view fvel, const double* farea);
+/* Autotuned chunk length (sources), work items per evaluation, padded
+ * targets. */
+int lpm_ensemble_info(lpm_ensemble* e, int64_t* chunk_len, int64_t* items,
+                      int64_t* targets);
+int lpm_ensemble_nbody_time(lpm_ensemble* e, double* ms, int64_t* launches);
+/* Fixes the chunk length (sources; rounded up to whole tiles) instead of
+ * autotuning it, e.g. for bitwise-reproducible runs across ensembles.  Call
+ * before the first velocity/step call. */
+int lpm_ensemble_set_chunk_len(lpm_ensemble* e, int64_t chunk_len);
+
 /* ---- host-side inputs: meshes and initial conditions -------------------- */
 /* Mesh kinds (restatements of the reference seeds' tree_init,
  * src/mesh/lpm_polymesh2d_impl.hpp:26-42, with the triangle and quad dividers

@@ -20,7 +20,7 @@ OUT = PKG / "_lib"
 LIB = OUT / "liblpm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu"]
+CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "ensemble.cu"]
 CXX_SOURCES = ["mesh.cpp", "ics.cpp"]
 
 

@@ -56,6 +56,9 @@ EXPORTS = [
     "lpm_ic2d_rk2_create", "lpm_ic2d_rk2_destroy", "lpm_ic2d_rk2_advance_timestep",
     "lpm_mesh_sizes", "lpm_mesh_build", "lpm_ic_eval", "lpm_measure_fma_peak",
     "lpm_bve_rk4_nbody_time", "lpm_ic2d_rk2_nbody_time", "lpm_bve_vertex_velocity_static",
+    "lpm_ensemble_create", "lpm_ensemble_destroy", "lpm_ensemble_velocity",
+    "lpm_ensemble_advance_timestep", "lpm_ensemble_info", "lpm_ensemble_nbody_time",
+    "lpm_ensemble_set_chunk_len",
 ]
 
 
@@ -124,6 +127,14 @@ def _declare(L: C.CDLL) -> None:
         "lpm_bve_rk4_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ic2d_rk2_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_bve_vertex_velocity_static": [V, V, i64, V, vp, vp, vp, i64, vp],
+        "lpm_ensemble_create": [vp, C.POINTER(C.c_void_p), i32, vp, vp, vp, dbl, dbl, dbl, i32,
+                                u32],
+        "lpm_ensemble_destroy": [vp],
+        "lpm_ensemble_velocity": [vp, V, V, V, vp, V, vp],
+        "lpm_ensemble_advance_timestep": [vp, V, vp, V, V, vp, V, vp],
+        "lpm_ensemble_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)],
+        "lpm_ensemble_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
+        "lpm_ensemble_set_chunk_len": [vp, i64],
     }
     for name, args in sig.items():
         f = getattr(L, name)

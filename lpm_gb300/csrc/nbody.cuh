@@ -128,42 +128,54 @@ struct TilePipe {
   uint64_t* bar;   // [2]
   const Rec* src;  // chunk start in global memory
   int ntiles;
+  unsigned g0 = 0;  // tiles this CTA consumed before the chunk (a persistent
+                    // CTA keeps the barriers' phases running across chunks)
 
-  __device__ void start() {
+  __device__ void init() {
     if (threadIdx.x == 0) {
       mbar_init(&bar[0], 1);
       mbar_init(&bar[1], 1);
       mbar_fence_init();
     }
     __syncthreads();
+  }
+  __device__ void prefetch() {
     if (threadIdx.x == 0) {
-      for (int b = 0; b < 2 && b < ntiles; ++b) issue(b, b);
+      for (int t = 0; t < 2 && t < ntiles; ++t) issue(t);
     }
   }
-  __device__ void issue(int tile, int b) {
+  __device__ void start() {
+    init();
+    prefetch();
+  }
+  __device__ void issue(int t) {
+    const unsigned b = (g0 + t) & 1;
     const unsigned bytes = TILE * sizeof(Rec);
     mbar_expect_tx(&bar[b], bytes);
-    tma_load_1d(buf + b * TILE, src + (int64_t)tile * TILE, bytes, &bar[b]);
+    tma_load_1d(buf + b * TILE, src + (int64_t)t * TILE, bytes, &bar[b]);
   }
   // Waits for tile t; returns false (CTA-uniform) if the wait gave up.
   __device__ bool acquire(int t) {
-    const bool ok = mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1);
+    const unsigned g = g0 + t;
+    const bool ok = mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1);
     return !__syncthreads_or(!ok);
   }
   // All threads are done with tile t: refill its buffer with tile t + 2.
   __device__ void release(int t) {
     __syncthreads();
-    if (threadIdx.x == 0 && t + 2 < ntiles) issue(t + 2, t & 1);
+    if (threadIdx.x == 0 && t + 2 < ntiles) issue(t + 2);
   }
   // After a timeout: wait (bounded) for copies still in flight, then return.
   __device__ void drain(int t, int* err) {
     if (threadIdx.x == 0) {
       atomicExch(err, 1);
-      for (int k = t; k < t + 2 && k < ntiles; ++k)
-        (void)mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1);
+      for (int k = t; k < t + 2 && k < ntiles; ++k) {
+        const unsigned g = g0 + k;
+        (void)mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1);
+      }
     }
   }
-  __device__ const Rec* tile(int t) const { return buf + (t & 1) * TILE; }
+  __device__ const Rec* tile(int t) const { return buf + ((g0 + t) & 1) * TILE; }
 };
 
 // ---------------------------------------------------------------------------
@@ -194,46 +206,25 @@ __device__ __forceinline__ void two_sum_acc(double& s, double& c, double p) {
 
 // SKIPC: in the stream-function sum, drop coincident pairs (q == c0, i.e.
 // d == 0: the skipped i == j term).  The velocity term of such a pair is 0.
-template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE>
-__global__ void __launch_bounds__(NT)
-    nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
-                const typename Vec4<T>::type* __restrict__ src, int64_t ntgt_pad,
-                int64_t nsrc_pad, int chunk_len, T c0, double* __restrict__ part,
-                int* err) {
+template <typename T, int NDIM, bool WU, bool WP>
+struct ChordAcc {
+  static constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
+};
+
+// Runs one chunk (pipe.ntiles tiles already prefetched) for R targets per
+// thread, accumulating into the compensated sums (S, C).  Returns false if a
+// tile wait gave up (the pipe has been drained and err set).
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int TILE>
+__device__ __forceinline__ bool chord_chunk(
+    TilePipe<typename Vec4<T>::type, TILE>& pipe, const T (&tx)[R], const T (&ty)[R],
+    const T (&tz)[R], T (&S)[ChordAcc<T, NDIM, WU, WP>::NC][R],
+    T (&C)[ChordAcc<T, NDIM, WU, WP>::NC][R], T c0, int* err) {
   using V4 = typename Vec4<T>::type;
-  constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
-  __shared__ __align__(128) V4 sbuf[2 * TILE];
-  __shared__ __align__(8) uint64_t sbar[2];
-
-  const int tid = threadIdx.x;
-  const int64_t tbase = (int64_t)blockIdx.x * (NT * R);
-  const int64_t s0 = (int64_t)blockIdx.y * chunk_len;
-  int64_t slen = nsrc_pad - s0;
-  if (slen > chunk_len) slen = chunk_len;
-
-  T tx[R], ty[R], tz[R];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const V4 t = tgt[tbase + r * NT + tid];
-    tx[r] = t.x;
-    ty[r] = t.y;
-    tz[r] = t.z;
-  }
-  T S[NC][R], C[NC][R];
-#pragma unroll
-  for (int k = 0; k < NC; ++k)
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      S[k][r] = T(0);
-      C[k][r] = T(0);
-    }
-
-  TilePipe<V4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
-  pipe.start();
+  constexpr int NC = ChordAcc<T, NDIM, WU, WP>::NC;
   for (int t = 0; t < pipe.ntiles; ++t) {
     if (!pipe.acquire(t)) {
       pipe.drain(t, err);
-      return;
+      return false;
     }
     const V4* sm = pipe.tile(t);
     T P[NC][R];
@@ -276,6 +267,46 @@ __global__ void __launch_bounds__(NT)
       for (int r = 0; r < R; ++r) two_sum_acc(S[k][r], C[k][r], P[k][r]);
     pipe.release(t);
   }
+  return true;
+}
+
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE>
+__global__ void __launch_bounds__(NT)
+    nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
+                const typename Vec4<T>::type* __restrict__ src, int64_t ntgt_pad,
+                int64_t nsrc_pad, int chunk_len, T c0, double* __restrict__ part,
+                int* err) {
+  using V4 = typename Vec4<T>::type;
+  constexpr int NC = ChordAcc<T, NDIM, WU, WP>::NC;
+  __shared__ __align__(128) V4 sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+
+  const int tid = threadIdx.x;
+  const int64_t tbase = (int64_t)blockIdx.x * (NT * R);
+  const int64_t s0 = (int64_t)blockIdx.y * chunk_len;
+  int64_t slen = nsrc_pad - s0;
+  if (slen > chunk_len) slen = chunk_len;
+
+  T tx[R], ty[R], tz[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const V4 t = tgt[tbase + r * NT + tid];
+    tx[r] = t.x;
+    ty[r] = t.y;
+    tz[r] = t.z;
+  }
+  T S[NC][R], C[NC][R];
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      S[k][r] = T(0);
+      C[k][r] = T(0);
+    }
+
+  TilePipe<V4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  pipe.start();
+  if (!chord_chunk<T, NDIM, WU, WP, SKIPC, R, TILE>(pipe, tx, ty, tz, S, C, c0, err)) return;
 
   double* out = part + (int64_t)blockIdx.y * NC * ntgt_pad;
 #pragma unroll
