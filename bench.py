@@ -507,6 +507,79 @@ def run_ensemble(args, device):
             "clocks": clocks, "gpu_launches": launches}
 
 
+def run_plane(args, device):
+    """Configuration C3: planar incompressible flow, colliding Lamb dipoles of
+    radius 1 and strength +-2 centred at (-+2, 0), uniform quad mesh of
+    [-4, 4]^2 at level 9 (1024 x 1024 leaf cells), eps = 0.02, RK2 dt = 0.01;
+    velocity and stream function at every evaluation (FP32C).  Accuracy: FP32C
+    vs the reference FP64 arithmetic on 16,384 seeded vertex targets."""
+    import torch
+
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.ic2d import Incompressible2D, Incompressible2DRK2, colliding_dipoles_params
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+    ic = Incompressible2D(core.MESH_QUAD_RECT, args.plane_level, radius=4.0, eps=0.02, ctx=ctx)
+    ic.init_vorticity(core.IC_DIPOLE_PAIR, colliding_dipoles_params())
+    ctx.set_precision(core.FP32C)
+    ic.init_direct_sums()
+    nv, nleaf = ic.n_vertices_host(), int((ic.host_face_mask == 0).sum())
+    ipe = (nv + nleaf) * nleaf
+    # accuracy on a target subsample, initial state
+    idx = torch.from_numpy(np.sort(np.random.default_rng(20261203).choice(nv, 16384, replace=False))).to(ic.vert_x.device)
+    xs = ic.vert_x[idx].contiguous()
+    outs = {}
+    for prec in (core.FP32C, core.FP64):
+        ctx.set_precision(prec)
+        u = torch.zeros(xs.shape[0], 2, dtype=torch.float64, device=xs.device)
+        p = torch.zeros(xs.shape[0], dtype=torch.float64, device=xs.device)
+        F.ic2d_passive_sums(ctx, u, p, xs, ic.face_x, ic.rel_vort_active, ic.face_area,
+                            ic.face_mask, ic.eps)
+        outs[prec] = (u, p)
+    torch.cuda.synchronize(device)
+    err = {"velocity": rel_errors(outs[core.FP32C][0], outs[core.FP64][0]),
+           "stream_fn": rel_errors(outs[core.FP32C][1], outs[core.FP64][1])}
+    solver = Incompressible2DRK2(0.01, ic, precision=core.FP32C,
+                                 flags=core.STEP_SKIP_MASKED_TARGETS)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        ic.advance_timestep(solver)
+    torch.cuda.synchronize(device)
+    sampler = ClockSampler(device)
+    sampler.start()
+    l0 = ctx.kernel_launches
+    ms = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ic.advance_timestep(solver)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        ms += a.elapsed_time(b)
+    clocks = sampler.stop()
+    inv = (ic.total_vorticity(), ic.total_enstrophy(), ic.total_kinetic_energy())
+    return {"metric": "incompressible2d RK2 Ginteractions/s (planar, velocity + stream function)",
+            "value": round(2 * ipe * args.steps / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (generated quad mesh + Lamb dipoles)",
+            "config": {"workload": f"planar colliding dipoles, quad level {args.plane_level} on "
+                                   "[-4,4]^2, eps=0.02, RK2 dt=0.01", "vertices": nv,
+                       "leaf_faces": nleaf, "interactions_per_step": 2 * ipe},
+            "errors_fp32c_vs_fp64_16384_vertex_targets": err,
+            "invariants_after": {"circulation": inv[0], "enstrophy": inv[1],
+                                 "kinetic_energy": inv[2]},
+            "clocks": clocks, "gpu_launches": ctx.kernel_launches - l0}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,8 +587,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--level", type=int, default=LEVEL)
-    ap.add_argument("--config", choices=["c2", "c4"], default="c2",
-                    help="c2: the metric's workload (default); c4: 256-problem ensemble")
+    ap.add_argument("--config", choices=["c2", "c3", "c4"], default="c2",
+                    help="c2: the metric's workload (default); c3: planar dipoles; "
+                         "c4: 256-problem ensemble")
+    ap.add_argument("--plane-level", type=int, default=9)
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--cpu-targets", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
@@ -540,6 +615,8 @@ def main():
         dist.init_process_group("nccl")
     if args.config == "c4":
         res = run_ensemble(args, local) if rank == 0 else {}
+    elif args.config == "c3":
+        res = run_plane(args, local) if rank == 0 else {}
     else:
         res = run_ours(args, rank, world, local)
     if rank == 0:

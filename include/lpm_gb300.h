@@ -110,7 +110,7 @@ int lpm_bve_vertex_velocity(lpm_context* ctx, lpm_view u, lpm_view vx,
  * callers that cannot allocate device memory: it calls no cudaMalloc or
  * cudaFree and needs no context.  Its scratch is one 64 MiB array inside the
  * library, held on every GPU that loads it until the process exits; problems
- * needing more (about 24 B per face slot + 40 B per target) are rejected with
+ * needing more (about 40 B per face slot + 44 B per target) are rejected with
  * LPM_ERR_ARG.  The first call on a device looks up the array's address; make
  * it before any stream capture.  Calls share the array: calls that overlap on
  * the GPU race.  Runs on `cuda_stream` and returns after it has finished. */

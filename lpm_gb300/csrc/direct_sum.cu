@@ -114,9 +114,9 @@ __global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
     g = (form == FORM_BVE && MODE == M_REF64) ? (-zeta[s]) * area[s] : zeta[s] * area[s];
   }
   if (MODE == M_C32) {
-    reinterpret_cast<float4*>(out)[k] = make_float4(
-        __double2float_rn(p0), __double2float_rn(p1), __double2float_rn(p2),
-        __double2float_rn(g));
+    reinterpret_cast<SrcF32*>(out)[k] =
+        make_src_f32(__double2float_rn(p0), __double2float_rn(p1),
+                     __double2float_rn(p2), __double2float_rn(g));
   } else {
     reinterpret_cast<double4*>(out)[k] = make_double4(p0, p1, p2, g);
   }
@@ -166,7 +166,7 @@ __global__ void k_sum_g_partial(const void* src, bool f32, int64_t n, double* pa
   double s = 0;
   for (int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * 256)
-    s += f32 ? (double)static_cast<const float4*>(src)[k].w
+    s += f32 ? (double)static_cast<const SrcF32*>(src)[k].b.z
              : static_cast<const double4*>(src)[k].w;
   sh[threadIdx.x] = s;
   __syncthreads();
@@ -249,9 +249,10 @@ void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
   constexpr bool F = std::is_same<T, float>::value;
   constexpr int NT = F ? F32_NT : F64_NT, R = F ? F32_R : F64_R, TILE = F ? F32_TILE : F64_TILE;
   using V4 = typename Vec4<T>::type;
+  using Rec = typename SrcRec<T>::type;
   dim3 grid(unsigned(p.ntgt_pad / (NT * R)), unsigned(p.nchunks));
   nbody_chord<T, NDIM, WU, WP, SKIPC, R, NT, TILE><<<grid, NT, 0, ctx.stream>>>(
-      static_cast<const V4*>(tgt), static_cast<const V4*>(src), p.ntgt_pad, p.nsrc_pad,
+      static_cast<const V4*>(tgt), static_cast<const Rec*>(src), p.ntgt_pad, p.nsrc_pad,
       p.chunk_len, c0, part, ctx.d_err);
   ctx.launches++;
 }
@@ -478,9 +479,10 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   // Upper bounds first, so one reservation covers the whole call.
   NbodyPlan p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
                            spec.want_psi, ntgt, src.nslots);
-  const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4);
+  const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4);  // target record
+  const size_t srec = 32;  // source record: SrcF32 or double4
   const size_t need = 4096 + sizeof(int) * (2 * size_t(src.nslots) + 2 * (size_t(src.nslots) / SCAN_BLOCK + 2)) +
-                      rec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
+                      srec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
                       sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes_max() +
                       sizeof(double) * 300 + 8 * 256;
   ctx.arena.reserve(need);
@@ -493,7 +495,7 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   for (int s = 0; s < nseg; ++s)
     if (segs[s].collocated && spec.skip_self) p.skipc = true;
 
-  void* srcp = ctx.arena.take(rec * size_t(p.nsrc_pad));
+  void* srcp = ctx.arena.take(srec * size_t(p.nsrc_pad));
   void* tgtp = ctx.arena.take(rec * size_t(p.ntgt_pad));
   int* tself = static_cast<int*>(ctx.arena.take(sizeof(int) * size_t(p.ntgt_pad)));
   double* part = static_cast<double*>(ctx.arena.take(p.part_bytes()));

@@ -35,18 +35,19 @@ template <typename T, int R, int NT, int TILE>
 __global__ void __launch_bounds__(NT)
     ens_nbody(const int4* __restrict__ items, int nitems, int* counter,
               const typename Vec4<T>::type* __restrict__ tgt,
-              const typename Vec4<T>::type* __restrict__ src, const int64_t* ptoff,
+              const typename SrcRec<T>::type* __restrict__ src, const int64_t* ptoff,
               const int64_t* ptpad, const int64_t* psoff, const int64_t* pspad,
               const int64_t* ppart, int chunk_len, T c0, double* __restrict__ part,
               int* err) {
   using V4 = typename Vec4<T>::type;
+  using Rec = typename SrcRec<T>::type;
   constexpr int NC = 3;
-  __shared__ __align__(128) V4 sbuf[2 * TILE];
+  __shared__ __align__(128) Rec sbuf[2 * TILE];
   __shared__ __align__(8) uint64_t sbar[2];
   __shared__ int s_item;
   const int tid = threadIdx.x;
 
-  TilePipe<V4, TILE> pipe{sbuf, sbar, src, 0};
+  TilePipe<Rec, TILE> pipe{sbuf, sbar, src, 0};
   pipe.init();
   for (;;) {
     if (tid == 0) s_item = atomicAdd(counter, 1);
@@ -216,9 +217,9 @@ struct lpm_ensemble {
     d_spad = static_cast<int64_t*>(upload(spad));
     const size_t rec = f32() ? 16 : 32;
     tgt = dalloc(rec * T);
-    src = dalloc(rec * S);
+    src = dalloc(32 * S);  // SrcF32 / double4
     LPM_CUDA(cudaMemset(tgt, 0, rec * T));
-    LPM_CUDA(cudaMemset(src, 0, rec * S));
+    LPM_CUDA(cudaMemset(src, 0, 32 * S));
     counter = static_cast<int*>(dalloc(sizeof(int)));
     buf = static_cast<double*>(dalloc(sizeof(double) * size_t(T) * 19));
     if (f32())
@@ -322,7 +323,7 @@ struct lpm_ensemble {
       lpm::ens_nbody<float, lpm::F32_R, lpm::F32_NT, lpm::F32_TILE>
           <<<grid, lpm::F32_NT, 0, c.stream>>>(
               items, int(nitems), counter, static_cast<const float4*>(tgt),
-              static_cast<const float4*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
+              static_cast<const lpm::SrcF32*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
               chunk_len, float(c0()), part, c.d_err);
     else
       lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE>

@@ -190,6 +190,46 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
 template <> struct Vec4<double> { using type = double4; };
 
+// FP32 source record with every value duplicated, (x, x, y, y) (z, z, g, g),
+// so that the packed f32x2 instructions apply one source to two targets
+// without re-packing it per pair.
+struct __align__(16) SrcF32 {
+  float4 a, b;
+};
+__host__ __device__ inline SrcF32 make_src_f32(float x, float y, float z, float g) {
+  return SrcF32{make_float4(x, x, y, y), make_float4(z, z, g, g)};
+}
+template <typename T> struct SrcRec;
+template <> struct SrcRec<float> { using type = SrcF32; };
+template <> struct SrcRec<double> { using type = double4; };
+
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction does the
+// operation on both halves of a 64-bit register pair.
+using u64 = unsigned long long;
+__device__ __forceinline__ u64 pk2(float lo, float hi) {
+  u64 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(u64 v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
+  u64 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+  u64 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+  u64 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 __device__ __forceinline__ float chord_rcp(float q) { return rcp_approx(q); }
 __device__ __forceinline__ double chord_rcp(double q) { return 1.0 / q; }
 __device__ __forceinline__ float chord_lg2(float q) { return lg2_approx(q); }
@@ -214,71 +254,149 @@ struct ChordAcc {
 // Runs one chunk (pipe.ntiles tiles already prefetched) for R targets per
 // thread, accumulating into the compensated sums (S, C).  Returns false if a
 // tile wait gave up (the pipe has been drained and err set).
+//
+// FP32: targets are processed in pairs (2h, 2h+1) with f32x2 instructions
+// against the duplicated source record: 5 packed FP32 instructions and one
+// MUFU reciprocal per pair instead of 10 scalar ones.  Each packed operation
+// is the two scalar operations, so the results are those of the scalar form.
 template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int TILE>
 __device__ __forceinline__ bool chord_chunk(
-    TilePipe<typename Vec4<T>::type, TILE>& pipe, const T (&tx)[R], const T (&ty)[R],
+    TilePipe<typename SrcRec<T>::type, TILE>& pipe, const T (&tx)[R], const T (&ty)[R],
     const T (&tz)[R], T (&S)[ChordAcc<T, NDIM, WU, WP>::NC][R],
     T (&C)[ChordAcc<T, NDIM, WU, WP>::NC][R], T c0, int* err) {
-  using V4 = typename Vec4<T>::type;
+  using Rec = typename SrcRec<T>::type;
   constexpr int NC = ChordAcc<T, NDIM, WU, WP>::NC;
-  for (int t = 0; t < pipe.ntiles; ++t) {
-    if (!pipe.acquire(t)) {
-      pipe.drain(t, err);
-      return false;
+  if constexpr (std::is_same<T, float>::value) {
+    static_assert(R % 2 == 0, "packed FP32 needs an even number of targets per thread");
+    constexpr int H = R / 2;
+    u64 TX[H], TY[H], TZ[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      TX[h] = pk2(tx[2 * h], tx[2 * h + 1]);
+      TY[h] = pk2(ty[2 * h], ty[2 * h + 1]);
+      TZ[h] = pk2(tz[2 * h], tz[2 * h + 1]);
     }
-    const V4* sm = pipe.tile(t);
-    T P[NC][R];
+    const u64 C02 = pk2(c0, c0);
+    for (int t = 0; t < pipe.ntiles; ++t) {
+      if (!pipe.acquire(t)) {
+        pipe.drain(t, err);
+        return false;
+      }
+      const Rec* sm = pipe.tile(t);
+      u64 P[NC][H];
 #pragma unroll
-    for (int k = 0; k < NC; ++k)
+      for (int k = 0; k < NC; ++k)
 #pragma unroll
-      for (int r = 0; r < R; ++r) P[k][r] = T(0);
+        for (int h = 0; h < H; ++h) P[k][h] = 0ull;
 
 #pragma unroll 4
-    for (int j = 0; j < TILE; ++j) {
-      const V4 s = sm[j];
+      for (int j = 0; j < TILE; ++j) {
+        const Rec s = sm[j];
+        const u64 sx = pk2(s.a.x, s.a.y), sy = pk2(s.a.z, s.a.w);
+        const u64 sz = pk2(s.b.x, s.b.y), sw = pk2(s.b.z, s.b.w);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const T dx = tx[r] - s.x;
-        const T dy = ty[r] - s.y;
-        T q;
-        T dz = T(0);
-        if (NDIM == 3) {
-          dz = tz[r] - s.z;
-          q = chord_fma(dx, dx, chord_fma(dy, dy, chord_fma(dz, dz, c0)));
-        } else {
-          q = chord_fma(dx, dx, chord_fma(dy, dy, c0));
-        }
-        if (WU) {
-          const T w = s.w * chord_rcp(q);
-          P[0][r] = chord_fma(w, dx, P[0][r]);
-          P[1][r] = chord_fma(w, dy, P[1][r]);
-          if (NDIM == 3) P[2][r] = chord_fma(w, dz, P[2][r]);
-        }
-        if (WP) {
-          T lg = chord_lg2(q);
-          if (SKIPC) lg = (q == c0) ? T(0) : lg;
-          P[NC - 1][r] = chord_fma(s.w, lg, P[NC - 1][r]);
+        for (int h = 0; h < H; ++h) {
+          const u64 dx = sub2(TX[h], sx);
+          const u64 dy = sub2(TY[h], sy);
+          u64 dz = 0ull;
+          u64 q;
+          if (NDIM == 3) {
+            dz = sub2(TZ[h], sz);
+            q = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, C02)));
+          } else {
+            q = fma2(dx, dx, fma2(dy, dy, C02));
+          }
+          float qa, qb;
+          upk2(q, qa, qb);
+          if (WU) {
+            const u64 w = mul2(sw, pk2(rcp_approx(qa), rcp_approx(qb)));
+            P[0][h] = fma2(w, dx, P[0][h]);
+            P[1][h] = fma2(w, dy, P[1][h]);
+            if (NDIM == 3) P[2][h] = fma2(w, dz, P[2][h]);
+          }
+          if (WP) {
+            float la = lg2_approx(qa), lb = lg2_approx(qb);
+            if (SKIPC) {
+              la = (qa == c0) ? 0.f : la;
+              lb = (qb == c0) ? 0.f : lb;
+            }
+            P[NC - 1][h] = fma2(sw, pk2(la, lb), P[NC - 1][h]);
+          }
         }
       }
+#pragma unroll
+      for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+          float pa, pb;
+          upk2(P[k][h], pa, pb);
+          two_sum_acc(S[k][2 * h], C[k][2 * h], pa);
+          two_sum_acc(S[k][2 * h + 1], C[k][2 * h + 1], pb);
+        }
+      pipe.release(t);
     }
+    return true;
+  } else {
+    for (int t = 0; t < pipe.ntiles; ++t) {
+      if (!pipe.acquire(t)) {
+        pipe.drain(t, err);
+        return false;
+      }
+      const Rec* sm = pipe.tile(t);
+      T P[NC][R];
 #pragma unroll
-    for (int k = 0; k < NC; ++k)
+      for (int k = 0; k < NC; ++k)
 #pragma unroll
-      for (int r = 0; r < R; ++r) two_sum_acc(S[k][r], C[k][r], P[k][r]);
-    pipe.release(t);
+        for (int r = 0; r < R; ++r) P[k][r] = T(0);
+
+#pragma unroll 4
+      for (int j = 0; j < TILE; ++j) {
+        const Rec s = sm[j];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const T dx = tx[r] - s.x;
+          const T dy = ty[r] - s.y;
+          T q;
+          T dz = T(0);
+          if (NDIM == 3) {
+            dz = tz[r] - s.z;
+            q = chord_fma(dx, dx, chord_fma(dy, dy, chord_fma(dz, dz, c0)));
+          } else {
+            q = chord_fma(dx, dx, chord_fma(dy, dy, c0));
+          }
+          if (WU) {
+            const T w = s.w * chord_rcp(q);
+            P[0][r] = chord_fma(w, dx, P[0][r]);
+            P[1][r] = chord_fma(w, dy, P[1][r]);
+            if (NDIM == 3) P[2][r] = chord_fma(w, dz, P[2][r]);
+          }
+          if (WP) {
+            T lg = chord_lg2(q);
+            if (SKIPC) lg = (q == c0) ? T(0) : lg;
+            P[NC - 1][r] = chord_fma(s.w, lg, P[NC - 1][r]);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NC; ++k)
+#pragma unroll
+        for (int r = 0; r < R; ++r) two_sum_acc(S[k][r], C[k][r], P[k][r]);
+      pipe.release(t);
+    }
+    return true;
   }
-  return true;
 }
 
 template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE>
 __global__ void __launch_bounds__(NT)
     nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
-                const typename Vec4<T>::type* __restrict__ src, int64_t ntgt_pad,
+                const typename SrcRec<T>::type* __restrict__ src, int64_t ntgt_pad,
                 int64_t nsrc_pad, int chunk_len, T c0, double* __restrict__ part,
                 int* err) {
   using V4 = typename Vec4<T>::type;
+  using Rec = typename SrcRec<T>::type;
   constexpr int NC = ChordAcc<T, NDIM, WU, WP>::NC;
-  __shared__ __align__(128) V4 sbuf[2 * TILE];
+  __shared__ __align__(128) Rec sbuf[2 * TILE];
   __shared__ __align__(8) uint64_t sbar[2];
 
   const int tid = threadIdx.x;
@@ -304,7 +422,7 @@ __global__ void __launch_bounds__(NT)
       C[k][r] = T(0);
     }
 
-  TilePipe<V4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  TilePipe<Rec, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
   pipe.start();
   if (!chord_chunk<T, NDIM, WU, WP, SKIPC, R, TILE>(pipe, tx, ty, tz, S, C, c0, err)) return;
 

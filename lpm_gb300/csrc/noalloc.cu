@@ -69,7 +69,7 @@ size_t fixed_need(int64_t nverts, int64_t nfaces) {
   const int64_t tpad = (nverts + 1023) / 1024 * 1024 + 1024;
   const int64_t spad = (nfaces + 511) / 512 * 512 + 512;
   return 4096 + sizeof(int) * (2 * size_t(nfaces) + 2 * (size_t(nfaces) / 1024 + 2)) +
-         16 * size_t(spad) + 16 * size_t(tpad) + sizeof(int) * size_t(tpad) +
+         32 * size_t(spad) + 16 * size_t(tpad) + sizeof(int) * size_t(tpad) +
          sizeof(double) * 300 + 8 * 256 + 16 * 256;
 }
 

@@ -134,7 +134,7 @@ __device__ void pack(const TG& g, const PK& k, int64_t t, const double* p,
     const float4 r = make_float4(__double2float_rn(p[0]), __double2float_rn(p[1]),
                                  __double2float_rn(p2), gw);
     static_cast<float4*>(k.tgt)[t] = make_float4(r.x, r.y, r.z, self ? gw : 0.f);
-    if (src >= 0) static_cast<float4*>(k.src)[src] = r;
+    if (src >= 0) static_cast<SrcF32*>(k.src)[src] = make_src_f32(r.x, r.y, r.z, gw);
   } else if (k.mode == M_C64) {
     const double gw = src >= 0 ? dm(z, area) : 0.0;
     static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, self ? gw : 0.0);

@@ -93,13 +93,13 @@ struct lpm_stepper_base {
     plan.skipc = skip_self;
     const size_t rec = precision == LPM_FP32C ? 16 : 32;  // float4 / double4
     tgt = dalloc(rec * plan.ntgt_pad);
-    src = dalloc(rec * plan.nsrc_pad);
+    src = dalloc(32 * plan.nsrc_pad);  // SrcF32 / double4
     tself = static_cast<int*>(dalloc(sizeof(int) * plan.ntgt_pad));
     part = static_cast<double*>(dalloc(plan.part_bytes()));
     sgbuf = static_cast<double*>(dalloc(sizeof(double) * (8 + 256)));
     // zero the padding records once (never rewritten); tself padding = -1
     zero(tgt, rec * plan.ntgt_pad);
-    zero(src, rec * plan.nsrc_pad);
+    zero(src, 32 * plan.nsrc_pad);
     LPM_CUDA(cudaMemsetAsync(tself, 0xff, sizeof(int) * plan.ntgt_pad, c.stream));
     LPM_CUDA(cudaStreamSynchronize(c.stream));
     LPM_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
