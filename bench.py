@@ -507,6 +507,76 @@ def run_ensemble(args, device):
             "clocks": clocks, "gpu_launches": launches}
 
 
+def run_c1(args, device):
+    """Configuration C1: plain FP64 BVE, icosahedral level 4 (5,120 leaf
+    faces, 2,562 vertices), Rossby-Haurwitz R=4 with omega = K = Omega/12.5,
+    eps = 0, 10 RK4 steps of dt = 0.01, the reference's arithmetic and
+    quirks (all face slots evaluated, facevort4, no reprojection).  Parity:
+    the whole run against the FP64 oracle; CPU baseline: the oracle's run."""
+    import torch
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import lpm_oracle
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+    from lpm_gb300.bve import BVERK4, BVESphere, rossby_haurwitz_params
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device, precision=core.FP64)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+    sph = BVESphere(4, ctx=ctx)
+    sph.init_vorticity(core.IC_RH54, rossby_haurwitz_params())
+    sph.init_velocity()
+    torch.cuda.synchronize(device)
+    ref = lpm_oracle.BVEState(sph.vert_x.cpu().numpy(), sph.rel_vort_verts.cpu().numpy(),
+                              sph.velocity_verts.cpu().numpy(), sph.face_x.cpu().numpy(),
+                              sph.rel_vort_faces.cpu().numpy(), sph.velocity_faces.cpu().numpy(),
+                              sph.host_face_area, sph.host_face_mask)
+    nv, nleaf = sph.n_vertices_host(), sph.n_leaves()
+    ipe = (nv + nleaf) * nleaf
+    st = BVERK4(0.01, sph, precision=core.FP64)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.kernel_launches
+    a.record(stream)
+    for _ in range(10):
+        st.advance_timestep(sph)
+    b.record(stream)
+    torch.cuda.synchronize(device)
+    ms = a.elapsed_time(b)
+    launches = ctx.kernel_launches - l0
+    threads = os.cpu_count() or 1
+    lpm_oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    for _ in range(10):
+        ref.step(0.01, OMEGA)
+    cpu_s = time.perf_counter() - t0
+    leaf = sph.host_face_mask == 0
+
+    def rel(g, r):
+        g, r = np.asarray(g), np.asarray(r)
+        return float(np.abs(g - r).max() / np.abs(r).max())
+
+    parity = {"vertex_positions": rel(sph.vert_x.cpu(), ref.vx),
+              "leaf_positions": rel(sph.face_x.cpu().numpy()[leaf], ref.fx[leaf]),
+              "vertex_velocity": rel(sph.velocity_verts.cpu(), ref.vvel),
+              "leaf_velocity": rel(sph.velocity_faces.cpu().numpy()[leaf], ref.fvel[leaf]),
+              "leaf_vorticity": rel(sph.rel_vort_faces.cpu().numpy()[leaf], ref.fzeta[leaf])}
+    return {"metric": METRIC, "value": round(40 * ipe / (ms * 1e-3) / 1e9, 4), "unit": UNIT,
+            "n_gpus": 1, "steps": 10, "warmup": 0, "ms_per_step": round(ms / 10, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (generated mesh + Rossby-Haurwitz wave)",
+            "config": {"workload": "BVE sphere icosahedral level 4 RK4, RH R=4, eps=0, dt=0.01, "
+                                   "10 steps, reference arithmetic (FP64)", "vertices": nv,
+                       "leaf_faces": nleaf, "interactions_per_step": 4 * ipe},
+            "parity_vs_oracle_after_10_steps": parity,
+            "cpu_baseline": {"value": round(40 * ipe / cpu_s / 1e9, 4), "unit": UNIT,
+                             "cores": threads, "kind": "port",
+                             "sample": "the whole 10-step run (all face slots as targets)"},
+            "gpu_launches": launches}
+
+
 def run_plane(args, device):
     """Configuration C3: planar incompressible flow, colliding Lamb dipoles of
     radius 1 and strength +-2 centred at (-+2, 0), uniform quad mesh of
@@ -587,9 +657,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--level", type=int, default=LEVEL)
-    ap.add_argument("--config", choices=["c2", "c3", "c4"], default="c2",
-                    help="c2: the metric's workload (default); c3: planar dipoles; "
-                         "c4: 256-problem ensemble")
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4"], default="c2",
+                    help="c2: the metric's workload (default); c1: FP64 level 4; "
+                         "c3: planar dipoles; c4: 256-problem ensemble")
     ap.add_argument("--plane-level", type=int, default=9)
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--cpu-targets", type=int, default=8192)
@@ -617,6 +687,8 @@ def main():
         res = run_ensemble(args, local) if rank == 0 else {}
     elif args.config == "c3":
         res = run_plane(args, local) if rank == 0 else {}
+    elif args.config == "c1":
+        res = run_c1(args, local) if rank == 0 else {}
     else:
         res = run_ours(args, rank, world, local)
     if rank == 0:

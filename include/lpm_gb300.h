@@ -161,6 +161,11 @@ int lpm_ic2d_invariants(lpm_context* ctx, int ndim, int64_t nfaces,
                         const double* zeta, lpm_view vel, const double* area,
                         const uint8_t* mask, double out[3]);
 
+/* SphereTangentFunctor (src/lpm_sphere_functions.hpp:59-78): udotx(i) =
+ * x(i,:) . u(i,:), the tangency diagnostic of a sphere velocity field. */
+int lpm_sphere_tangency(lpm_context* ctx, double* udotx, lpm_view x, lpm_view u,
+                        int64_t n);
+
 /* ---- ErrNorms (src/lpm_error.hpp:81-91) -------------------------------- */
 /* Relative l1, l2 (weighted by wt; wt may be null = 1) and linf
  * (max|err|/max|exact|) of vector magnitudes (ndim > 1) or values (ndim 1);

@@ -58,7 +58,7 @@ EXPORTS = [
     "lpm_bve_rk4_nbody_time", "lpm_ic2d_rk2_nbody_time", "lpm_bve_vertex_velocity_static",
     "lpm_ensemble_create", "lpm_ensemble_destroy", "lpm_ensemble_velocity",
     "lpm_ensemble_advance_timestep", "lpm_ensemble_info", "lpm_ensemble_nbody_time",
-    "lpm_ensemble_set_chunk_len",
+    "lpm_ensemble_set_chunk_len", "lpm_sphere_tangency",
 ]
 
 
@@ -135,6 +135,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ensemble_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)],
         "lpm_ensemble_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ensemble_set_chunk_len": [vp, i64],
+        "lpm_sphere_tangency": [vp, vp, V, V, i64],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -380,6 +380,21 @@ int lpm_ic2d_tendencies(lpm_context* ctx, int ndim, double* dzeta, lpm_view u,
   }
 }
 
+int lpm_sphere_tangency(lpm_context* ctx, double* udotx, lpm_view x, lpm_view u,
+                        int64_t n) {
+  try {
+    if (int r = check_ctx(ctx)) return r;
+    if (bad_count(n)) return fail(LPM_ERR_ARG, "count out of range");
+    if (n > 0 && !udotx) return fail(LPM_ERR_ARG, "null output");
+    if (int r = check_view(x, n, "positions", false)) return r;
+    if (int r = check_view(u, n, "velocity", false)) return r;
+    lpm::tangency(*ctx, udotx, lpm::to_view(x), lpm::to_view(u), n);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
 int lpm_ic2d_invariants(lpm_context* ctx, int ndim, int64_t nfaces,
                         const double* zeta, lpm_view vel, const double* area,
                         const uint8_t* mask, double out[3]) {

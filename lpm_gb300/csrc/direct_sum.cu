@@ -243,18 +243,44 @@ void combine_dispatch(lpm_context& ctx, const NbodyPlan& p, const double* part,
     launch_combine<MODE, NDIM, false, true>(ctx, p, part, off, seg, tgt, sg, c0);
 }
 
-template <typename T, int NDIM, bool WU, bool WP, bool SKIPC>
-void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
-                    const void* src, double* part, T c0) {
-  constexpr bool F = std::is_same<T, float>::value;
-  constexpr int NT = F ? F32_NT : F64_NT, R = F ? F32_R : F64_R, TILE = F ? F32_TILE : F64_TILE;
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int MINB>
+void launch_chord_shape(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                        const void* src, double* part, T c0) {
+  constexpr int TILE = std::is_same<T, float>::value ? F32_TILE : F64_TILE;
   using V4 = typename Vec4<T>::type;
   using Rec = typename SrcRec<T>::type;
   dim3 grid(unsigned(p.ntgt_pad / (NT * R)), unsigned(p.nchunks));
-  nbody_chord<T, NDIM, WU, WP, SKIPC, R, NT, TILE><<<grid, NT, 0, ctx.stream>>>(
+  nbody_chord<T, NDIM, WU, WP, SKIPC, R, NT, TILE, MINB><<<grid, NT, 0, ctx.stream>>>(
       static_cast<const V4*>(tgt), static_cast<const Rec*>(src), p.ntgt_pad, p.nsrc_pad,
       p.chunk_len, c0, part, ctx.d_err);
   ctx.launches++;
+}
+
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC>
+void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+                    const void* src, double* part, T c0) {
+  if constexpr (std::is_same<T, float>::value) {
+    static_assert(kF32Shapes[0].nt == 256 && kF32Shapes[0].r == 4 && kF32Shapes[0].minb == 3 &&
+                      kF32Shapes[1].nt == 256 && kF32Shapes[1].r == 4 && kF32Shapes[1].minb == 4 &&
+                      kF32Shapes[2].nt == 128 && kF32Shapes[2].r == 8 && kF32Shapes[2].minb == 4 &&
+                      kF32Shapes[3].nt == 256 && kF32Shapes[3].r == 2 && kF32Shapes[3].minb == 5,
+                  "launch table out of sync with kF32Shapes");
+    switch (p.shape) {
+      case 1:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 4, 256, 4>(ctx, p, tgt, src, part, c0);
+        break;
+      case 2:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 8, 128, 4>(ctx, p, tgt, src, part, c0);
+        break;
+      case 3:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 2, 256, 5>(ctx, p, tgt, src, part, c0);
+        break;
+      default:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 4, 256, 3>(ctx, p, tgt, src, part, c0);
+    }
+  } else {
+    launch_chord_shape<T, NDIM, WU, WP, SKIPC, F64_R, F64_NT, 4>(ctx, p, tgt, src, part, c0);
+  }
 }
 
 template <typename T, int NDIM, bool WU, bool WP>
@@ -305,11 +331,10 @@ int occupancy(int precision) {
   if (o == 0) {
     int v = 0;
     if (m == M_C32)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_chord<float, 3, true, false, false, F32_R, F32_NT, F32_TILE>, F32_NT, 0);
+      v = 4;  // FP32 shapes share a fixed chunking (plan_nbody)
     else if (m == M_C64)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_chord<double, 3, true, false, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
+          &v, nbody_chord<double, 3, true, false, false, F64_R, F64_NT, F64_TILE, 4>, F64_NT, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &v, nbody_f64<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
@@ -357,7 +382,7 @@ NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
   p.wp = wp;
   p.ncomp = (wu ? ndim : 0) + (wp ? 1 : 0);
   const bool f32 = precision == LPM_FP32C;
-  const int tb = f32 ? F32_NT * F32_R : F64_NT * F64_R;
+  const int tb = f32 ? F32_TB : F64_NT * F64_R;
   const int tile = f32 ? F32_TILE : F64_TILE;
   p.ntgt = ntgt;
   p.ntgt_pad = std::max<int64_t>(tb, (ntgt + tb - 1) / tb * tb);
@@ -365,8 +390,10 @@ NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
   p.nsrc_pad = std::max<int64_t>(tile, (nsrc + tile - 1) / tile * tile);
   const int64_t ntb = p.ntgt_pad / tb;
   const int64_t ntiles = p.nsrc_pad / tile;
-  // Aim for ~16 waves of CTAs so the tail of the last wave stays small.
-  const int64_t slots = int64_t(std::max(ctx.num_sms, 1)) * occupancy(precision);
+  // Aim for ~16 waves of CTAs so the tail of the last wave stays small.  The
+  // FP32 shapes share one chunking (4 CTAs of 1024 targets per SM) so that the
+  // autotuner can swap shapes without changing the partial layout.
+  const int64_t slots = int64_t(std::max(ctx.num_sms, 1)) * (f32 ? 4 : occupancy(precision));
   int64_t nch = (16 * slots + ntb - 1) / ntb;
   if (ctx.max_part_bytes > 0) {
     const int64_t per_chunk = int64_t(sizeof(double)) * p.ncomp * p.ntgt_pad;
@@ -410,6 +437,50 @@ void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
   LPM_CUDA(cudaGetLastError());
 }
 
+int tune_shape(lpm_context& ctx, const NbodyPlan& p0, const void* tgt, const int* tself,
+               const void* src, double* part, double eps) {
+  if (p0.precision != LPM_FP32C) return 0;
+  auto lg = [](int64_t v) {
+    int k = 0;
+    while ((int64_t(1) << k) < v) ++k;
+    return uint64_t(k);
+  };
+  const uint64_t key = (uint64_t(p0.ndim) << 60) | (uint64_t(p0.wu) << 59) |
+                       (uint64_t(p0.wp) << 58) | (uint64_t(p0.skipc) << 57) |
+                       (lg(p0.ntgt_pad) << 8) | lg(p0.nsrc_pad);
+  auto it = ctx.tuned.find(key);
+  if (it != ctx.tuned.end()) return it->second;
+  // below ~2e9 pairs a launch lasts a few hundred microseconds: keep the default
+  if (!ctx.autotune || double(p0.ntgt_pad) * double(p0.nsrc_pad) < 2e9) {
+    ctx.tuned[key] = 0;
+    return 0;
+  }
+  cudaEvent_t e0, e1;
+  LPM_CUDA(cudaEventCreate(&e0));
+  LPM_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int sh = 0; sh < kNumF32Shapes; ++sh) {
+    NbodyPlan p = p0;
+    p.shape = sh;
+    launch_nbody(ctx, p, tgt, tself, src, part, eps);  // warm
+    LPM_CUDA(cudaEventRecord(e0, ctx.stream));
+    launch_nbody(ctx, p, tgt, tself, src, part, eps);
+    LPM_CUDA(cudaEventRecord(e1, ctx.stream));
+    LPM_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    LPM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = sh;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx.tuned[key] = best;
+  return best;
+}
+
 void sum_strengths(lpm_context& ctx, const void* src, bool f32, int64_t nsrc,
                    double* out, double* scratch256) {
   k_sum_g_partial<<<256, 256, 0, ctx.stream>>>(src, f32, nsrc, scratch256);
@@ -449,7 +520,9 @@ void pack_and_launch(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
     sum_strengths(ctx, srcp, MODE == M_C32, p.nsrc, sgp, sgp + 8);
   LPM_CUDA(cudaGetLastError());
 
-  launch_nbody(ctx, p, tgtp, tself, srcp, part, spec.eps);
+  NbodyPlan pt = p;
+  pt.shape = tune_shape(ctx, p, tgtp, tself, srcp, part, spec.eps);
+  launch_nbody(ctx, pt, tgtp, tself, srcp, part, spec.eps);
 
   const double c0 = MODE == M_C32 ? double(f32_c0(ndim, spec.eps)) : chord_c0(ndim, spec.eps);
   off = 0;
@@ -520,6 +593,13 @@ __global__ void k_bve_tendency(double* dz, View u, int64_t n, double dt,
                                double Omega) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dz[i] = __dmul_rn(__dmul_rn(__dmul_rn(-2.0, Omega), u(i, 2)), dt);
+}
+
+__global__ void k_tangency(double* out, View x, View u, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = __dadd_rn(__dadd_rn(__dmul_rn(x(i, 0), u(i, 0)), __dmul_rn(x(i, 1), u(i, 1))),
+                       __dmul_rn(x(i, 2), u(i, 2)));
 }
 
 __global__ void k_ic2d_tendency(double* dz, View u, int64_t n, int ndim,
@@ -637,6 +717,13 @@ void bve_tendency(lpm_context& ctx, double* dzeta, View u, int64_t n,
                   double dt, double Omega) {
   if (n == 0) return;
   k_bve_tendency<<<(n + 255) / 256, 256, 0, ctx.stream>>>(dzeta, u, n, dt, Omega);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+void tangency(lpm_context& ctx, double* out, View x, View u, int64_t n) {
+  if (n == 0) return;
+  k_tangency<<<(n + 255) / 256, 256, 0, ctx.stream>>>(out, x, u, n);
   ctx.launches++;
   LPM_CUDA(cudaGetLastError());
 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 
@@ -86,6 +87,8 @@ struct lpm_context {
   lpm::Arena arena;
   int64_t launches = 0;
   size_t max_part_bytes = 0;  // cap on chunk-partial scratch (0 = none)
+  std::map<uint64_t, int> tuned;  // autotuned FP32 kernel shape per size class
+  bool autotune = true;
 };
 
 namespace lpm {
@@ -140,6 +143,7 @@ struct NbodyPlan {
   int nchunks;
   int chunk_len;
   int nchunks_max;     // bound on nchunks for any nsrc <= this plan's nsrc
+  int shape = 0;       // FP32 kernel shape (index into kF32Shapes)
   bool skipc = false;  // chord stream function: drop coincident (i == j) pairs
   size_t part_bytes() const {
     return sizeof(double) * size_t(ncomp) * size_t(nchunks) * size_t(ntgt_pad);
@@ -155,6 +159,11 @@ NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
 void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
                   const int* tself, const void* src, double* part,
                   double eps);
+// FP32 plans: times every kernel shape on the packed arrays (one warm and
+// one timed launch each) and returns the fastest; synchronises.  Results are
+// cached in the context by problem size class.
+int tune_shape(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
+               const int* tself, const void* src, double* part, double eps);
 // FP32 squared-distance offset c0 (2 eps^2 on the sphere, eps^2 on the plane,
 // plus the 1e-30 floor).
 float f32_c0(int ndim, double eps);
@@ -169,6 +178,7 @@ void bve_tendency(lpm_context& ctx, double* dzeta, View u, int64_t n,
                   double dt, double Omega);
 void ic2d_tendency(lpm_context& ctx, int ndim, double* dzeta, View u,
                    int64_t n, double cor);
+void tangency(lpm_context& ctx, double* out, View x, View u, int64_t n);
 void invariants(lpm_context& ctx, int ndim, int64_t n, const double* zeta,
                 View vel, const double* area, const uint8_t* mask,
                 double out[3]);

@@ -387,8 +387,9 @@ __device__ __forceinline__ bool chord_chunk(
   }
 }
 
-template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE>
-__global__ void __launch_bounds__(NT)
+template <typename T, int NDIM, bool WU, bool WP, bool SKIPC, int R, int NT, int TILE,
+          int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     nbody_chord(const typename Vec4<T>::type* __restrict__ tgt,
                 const typename SrcRec<T>::type* __restrict__ src, int64_t ntgt_pad,
                 int64_t nsrc_pad, int chunk_len, T c0, double* __restrict__ part,
@@ -608,9 +609,25 @@ __device__ __forceinline__ void chord_epilogue(const double* a, const double* p,
   }
 }
 
-// Launch shapes.  FP32: 256 threads x 4 targets, 512-source tiles (8 KB per
-// buffer).  FP64 (both forms): 128 threads x 2 targets, 256-source tiles.
+// Launch shapes.  FP32: 512-source tiles (32-byte duplicated records, 16 KB
+// per buffer), target blocks of up to 1024; the default shape is 256 threads x
+// 4 targets, and plan-time autotuning picks one of kF32Shapes.  FP64 (both
+// forms): 128 threads x 2 targets, 256-source tiles (8 KB).
 constexpr int F32_NT = 256, F32_R = 4, F32_TILE = 512;
+constexpr int F32_TB = 1024;  // target padding: every FP32 shape divides it
 constexpr int F64_NT = 128, F64_R = 2, F64_TILE = 256;
+
+// FP32 kernel shapes: threads, targets per thread, minimum resident CTAs per
+// SM (a register cap through __launch_bounds__).
+struct F32Shape {
+  int nt, r, minb;
+};
+constexpr int kNumF32Shapes = 4;
+constexpr F32Shape kF32Shapes[kNumF32Shapes] = {
+    {256, 4, 3},  // <= 85 registers: 24 warps / SM
+    {256, 4, 4},  // <= 64 registers: 32 warps / SM
+    {128, 8, 4},  // <= 128 registers: 16 warps, 8 targets per source load
+    {256, 2, 5},  // <= 51 registers: 40 warps / SM
+};
 
 }  // namespace lpm

@@ -66,7 +66,7 @@ DeviceScratch& scratch_for(int dev) {
 // Bytes the vertex-velocity sum needs besides the chunk partials (an upper
 // bound; direct_sum asks the arena for the same items).
 size_t fixed_need(int64_t nverts, int64_t nfaces) {
-  const int64_t tpad = (nverts + 1023) / 1024 * 1024 + 1024;
+  const int64_t tpad = (nverts + 1023) / 1024 * 1024 + 1024;  // FP32 target blocks of 1024
   const int64_t spad = (nfaces + 511) / 512 * 512 + 512;
   return 4096 + sizeof(int) * (2 * size_t(nfaces) + 2 * (size_t(nfaces) / 1024 + 2)) +
          32 * size_t(spad) + 16 * size_t(tpad) + sizeof(int) * size_t(tpad) +
@@ -122,6 +122,7 @@ extern "C" int lpm_bve_vertex_velocity_static(lpm_view u, lpm_view vx, int64_t n
     ctx.arena.cap = cap;
     ctx.arena.fixed = true;
     ctx.max_part_bytes = cap - base_need - 256;
+    ctx.autotune = false;  // no per-call timing runs: the default kernel shape
     LPM_CUDA(cudaMemsetAsync(ctx.d_err, 0, sizeof(int), ctx.stream));
 
     lpm::SumSpec spec{3, lpm::FORM_BVE, LPM_FP32C, 0.0, true, false, true};

@@ -102,6 +102,8 @@ struct lpm_stepper_base {
     zero(src, 32 * plan.nsrc_pad);
     LPM_CUDA(cudaMemsetAsync(tself, 0xff, sizeof(int) * plan.ntgt_pad, c.stream));
     LPM_CUDA(cudaStreamSynchronize(c.stream));
+    // kernel shape for this problem size (the zeroed tiles time like real ones)
+    plan.shape = lpm::tune_shape(c, plan, tgt, tself, src, part, eps);
     LPM_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     ready = true;
   }

@@ -88,6 +88,11 @@ def ic2d_tendencies(ctx, dzeta, u, cor):
     check(lib().lpm_ic2d_tendencies(ctx.handle, int(u.shape[1]), ptr(dzeta), view(u), _n(u), cor))
 
 
+def sphere_tangency(ctx, udotx, x, u):
+    """SphereTangentFunctor (src/lpm_sphere_functions.hpp:59-78): x . u per point."""
+    check(lib().lpm_sphere_tangency(ctx.handle, ptr(udotx), view(x), view(u), _n(x)))
+
+
 def ic2d_invariants(ctx, zeta, vel, area, mask):
     import ctypes as C
     out = (C.c_double * 3)()

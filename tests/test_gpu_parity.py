@@ -242,6 +242,11 @@ def test_tendencies_and_invariants(gpu_ctx, oracle):
              0.5 * ((u * u).sum(1) * fa)[leaf].sum()]
     for a, b, s in zip(inv, ref, scale):
         assert abs(a - b) <= 1e-13 * s
+    tg = torch.zeros(fx.shape[0], dtype=torch.float64, device="cuda")
+    F.sphere_tangency(ctx, tg, dev(fx), dev(u))
+    ctx.synchronize()
+    assert np.array_equal(tg.cpu().numpy(),
+                          (fx[:, 0] * u[:, 0] + fx[:, 1] * u[:, 1]) + fx[:, 2] * u[:, 2])
     en = F.err_norms(ctx, dev(u + 1e-3), dev(u), dev(fa), dev(fm))
     er = oracle.err_norms(u + 1e-3, u, fa, fm)
     assert np.allclose(en, er, rtol=1e-12)
