@@ -299,6 +299,71 @@ int lpm_ic_eval(int kind, const double* params, int nparams, int ndim,
  * register-only microbenchmark; synchronous. */
 int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops);
 
+/* ---- octree far field with a learned correction ------------------------- */
+/* No reference counterpart: the reference's octree sources (LpmOctree*,
+ * LpmNodeArray*) are not built and src/tree/lpm_cpu_tree's generators are
+ * never called.  This is an alternative evaluator of the BVE sphere velocity
+ * (the sum of BVEVertexVelocity / BVEFaceVelocity, chord form with smoothing
+ * eps): an octree over the sources (leaves of <= leaf_max points), a target
+ * block of 128 Morton-ordered targets accepts a cell when
+ * h <= theta * (distance - block radius); accepted cells use the order-4
+ * Cartesian expansion of the kernel about the cell centre, the rest of the
+ * tree down to the leaves is summed exactly (FP32 compensated).  With a
+ * trained network enabled, every accepted cell with h / (distance - block
+ * radius) >= rho_min also gets the network's prediction of the expansion's
+ * residual (BF16 MLP on tcgen05 tensor cores).  A target block whose
+ * interaction lists overflow falls back to the full direct sum. */
+#define LPM_FF_NPARAM 40960 /* FP32 master weights: W1 128x48, W2 128x128,
+                               W3 128x128, W4 16x128, row-major */
+#define LPM_FF_NNORM 97     /* input mean[48], input 1/std[48], output scale */
+#define LPM_FF_NIN 48       /* network inputs (feature 40 is the constant 1) */
+typedef struct lpm_farfield lpm_farfield;
+int lpm_farfield_create(lpm_context* ctx, lpm_farfield** out, double theta,
+                        int leaf_max, double rho_min);
+int lpm_farfield_destroy(lpm_farfield* ff);
+/* Velocity at nx targets x (device, strided) from the face slots fx/zeta/
+ * area/mask (nf slots, the BVEFaceVelocity source arguments).  Builds the
+ * tree for these positions (host sort, synchronises) and evaluates. */
+int lpm_farfield_velocity(lpm_farfield* ff, lpm_view u, lpm_view x,
+                          int64_t nx, lpm_view fx, const double* zeta,
+                          const double* area, const uint8_t* mask, int64_t nf,
+                          double eps);
+/* Trains the network on nsamples (cell, target) samples drawn from seeded
+ * random vortex fields on icosahedral meshes of levels level_min..level_max
+ * (the exact FP64 cell sum minus the expansion is the target), with Adam,
+ * cosine learning rate, the given batch (a multiple of 128) and epochs.
+ * loss (optional, epochs floats) receives the mean loss per epoch.  Enables
+ * the network. */
+int lpm_farfield_train(lpm_farfield* ff, int64_t nsamples, int epochs,
+                       int batch, double lr, uint64_t seed, int level_min,
+                       int level_max, double eps, float* loss);
+int lpm_farfield_set_network(lpm_farfield* ff, int enable);
+/* HOST buffers of LPM_FF_NPARAM and LPM_FF_NNORM floats. */
+int lpm_farfield_get_weights(lpm_farfield* ff, float* w, float* norm);
+int lpm_farfield_set_weights(lpm_farfield* ff, const float* w,
+                             const float* norm);
+/* Gradient of the mean squared error (sum over the 3 outputs, mean over n
+ * rows, n a multiple of 128) with respect to the master weights, from the
+ * tensor-core training kernel: x = HOST n x 48 normalised inputs (rounded to
+ * BF16), y = HOST n x 3 targets, grad = HOST LPM_FF_NPARAM floats. */
+int lpm_farfield_grad(lpm_farfield* ff, const float* x, const float* y, int n,
+                      float* grad);
+/* Of the last evaluation: far (block, cell) pairs, near (target, source)
+ * pairs / 128, learned tiles, blocks on the direct-sum fallback, cells,
+ * target blocks.  out: 6 int64.  Synchronous. */
+int lpm_farfield_stats(lpm_farfield* ff, int64_t* out);
+/* Evaluate BVERK4 stages with the far field instead of the direct sum
+ * (precision LPM_FP64_CHORD steppers; the tree is built on the first step and
+ * rebuilt every rebuild_every steps, 0 = never).  ff must outlive st. */
+int lpm_bve_rk4_set_farfield(lpm_bve_rk4* st, lpm_farfield* ff,
+                             int rebuild_every);
+/* tcgen05 operand-layout self-test: D (128 x N) = A * B on the tensor cores,
+ * A 128 x K (a_mn = 0) or K x 128 (a_mn = 1), B N x K (b_mn = 0) or K x N
+ * (b_mn = 1), row-major FP32 device arrays rounded to BF16; N, K multiples of
+ * 16 in [16, 128]. */
+int lpm_tc_selftest(lpm_context* ctx, const float* A, const float* B, float* D,
+                    int N, int K, int a_mn, int b_mn);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,8 +20,9 @@ OUT = PKG / "_lib"
 LIB = OUT / "liblpm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "ensemble.cu"]
-CXX_SOURCES = ["mesh.cpp", "ics.cpp"]
+CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "ensemble.cu", "farfield.cu",
+              "mlp.cu", "ffapi.cu"]
+CXX_SOURCES = ["mesh.cpp", "ics.cpp", "tree.cpp"]
 
 
 def nvcc() -> str:

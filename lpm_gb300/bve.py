@@ -115,6 +115,12 @@ class BVERK4:
             ptr(sph.face_area), ptr(sph.face_mask)))
         sph.t += self.dt
 
+    def set_farfield(self, ff, rebuild_every: int = 0) -> None:
+        """Evaluate the stages with an octree far field (FP64_CHORD steppers)."""
+        check(lib().lpm_bve_rk4_set_farfield(self._h, ff.handle if ff is not None else None,
+                                             int(rebuild_every)))
+        self._ff = ff  # keep it alive as long as the stepper
+
     def nbody_time(self) -> tuple[float, int]:
         """(ms, launches) of the N-body kernels timed since the last call
         (requires core.STEP_TIME_NBODY)."""

@@ -59,6 +59,9 @@ EXPORTS = [
     "lpm_ensemble_create", "lpm_ensemble_destroy", "lpm_ensemble_velocity",
     "lpm_ensemble_advance_timestep", "lpm_ensemble_info", "lpm_ensemble_nbody_time",
     "lpm_ensemble_set_chunk_len", "lpm_sphere_tangency",
+    "lpm_farfield_create", "lpm_farfield_destroy", "lpm_farfield_velocity", "lpm_farfield_train",
+    "lpm_farfield_set_network", "lpm_farfield_get_weights", "lpm_farfield_set_weights",
+    "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest",
 ]
 
 
@@ -136,6 +139,17 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ensemble_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ensemble_set_chunk_len": [vp, i64],
         "lpm_sphere_tangency": [vp, vp, V, V, i64],
+        "lpm_farfield_create": [vp, C.POINTER(C.c_void_p), dbl, i32, dbl],
+        "lpm_farfield_destroy": [vp],
+        "lpm_farfield_velocity": [vp, V, V, i64, V, vp, vp, vp, i64, dbl],
+        "lpm_farfield_train": [vp, i64, i32, i32, dbl, C.c_uint64, i32, i32, dbl, vp],
+        "lpm_farfield_set_network": [vp, i32],
+        "lpm_farfield_get_weights": [vp, vp, vp],
+        "lpm_farfield_set_weights": [vp, vp, vp],
+        "lpm_farfield_grad": [vp, vp, vp, i32, vp],
+        "lpm_farfield_stats": [vp, vp],
+        "lpm_bve_rk4_set_farfield": [vp, vp, i32],
+        "lpm_tc_selftest": [vp, vp, vp, vp, i32, i32, i32, i32],
     }
     for name, args in sig.items():
         f = getattr(L, name)

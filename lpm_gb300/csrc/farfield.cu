@@ -1,0 +1,502 @@
+// farfield.cu -- octree evaluation of the BVE sphere velocity sum.
+//
+// Per evaluation (all on the context stream, capturable in a CUDA graph):
+//   k_ff_sort_src   packed double4 sources -> Morton-ordered float4
+//   k_ff_cells      per cell: centre, radius, frame, moments to order 4
+//                   (FP32 per 32-point batch, FP64 across batches and threads)
+//   k_ff_tblocks    per block of 128 Morton-ordered targets: centre, radius
+//   k_ff_lists      per target block: tree walk with the opening criterion
+//                   h <= theta (D - r_b): far cells, near leaves, and the far
+//                   cells close enough (h / (D - r_b) >= rho_min) for the
+//                   learned correction; a block whose lists overflow is
+//                   marked for the direct sum
+//   k_ff_eval       per target block: exact FP32 chord sum over the near
+//                   leaves (per-leaf partials merged by TwoSum) + order-4
+//                   expansion of the far cells, or the full direct sum for
+//                   a marked block; writes FP64 w
+//   k_ff_mlp        (mlp.cu) learned correction on tensor cores, adds to w
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "farfield_dev.cuh"
+#include "ffmath.cuh"
+#include "nbody.cuh"
+
+namespace lpm {
+
+namespace {
+
+__global__ void k_ff_sort_src(const double4* __restrict__ src, const int* __restrict__ perm,
+                              int64_t n, float4* __restrict__ ys) {
+  const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  const double4 s = src[perm[k]];
+  ys[k] = make_float4(float(s.x), float(s.y), float(s.z), float(s.w));
+}
+
+// Fixed-order block reduction of nv doubles held by each of 128 threads.
+template <int NV>
+__device__ void block_sum128(double* v, double* sh) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    double x = v[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[w * NV + i] = x;
+  }
+  __syncthreads();
+  if (t < NV) sh[4 * NV + t] = ((sh[t] + sh[NV + t]) + (sh[2 * NV + t] + sh[3 * NV + t]));
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = sh[4 * NV + i];
+  __syncthreads();
+}
+
+__device__ double block_max128(double x, double* sh) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+  if (lane == 0) sh[w] = x;
+  __syncthreads();
+  x = fmax(fmax(sh[0], sh[1]), fmax(sh[2], sh[3]));
+  __syncthreads();
+  return x;
+}
+
+// One CTA (128 threads) per cell.
+__global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
+                                                  const int4* __restrict__ cells, int ncells,
+                                                  float* __restrict__ cd) {
+  __shared__ double sh[5 * 40];
+  const int cell = blockIdx.x;
+  if (cell >= ncells) return;
+  const int4 ci = cells[cell];
+  const int s0 = ci.x, n = ci.y, t = threadIdx.x;
+  // pass 1: centre, S, sum g
+  double a[5] = {0, 0, 0, 0, 0};
+  for (int i = t; i < n; i += 128) {
+    const float4 p = ys[s0 + i];
+    a[0] += p.x;
+    a[1] += p.y;
+    a[2] += p.z;
+    a[3] += fabs((double)p.w);
+    a[4] += p.w;
+  }
+  block_sum128<5>(a, sh);
+  const double c[3] = {a[0] / n, a[1] / n, a[2] / n};
+  const double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  double q[9];
+  {
+    double nn[3] = {1, 0, 0};
+    if (cn > 0) nn[0] = c[0] / cn, nn[1] = c[1] / cn, nn[2] = c[2] / cn;
+    const double r[3] = {fabs(nn[2]) < 0.9 ? 0.0 : 1.0, 0.0, fabs(nn[2]) < 0.9 ? 1.0 : 0.0};
+    double e1[3] = {r[1] * nn[2] - r[2] * nn[1], r[2] * nn[0] - r[0] * nn[2], r[0] * nn[1] - r[1] * nn[0]};
+    const double l = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    e1[0] /= l, e1[1] /= l, e1[2] /= l;
+    const double e2[3] = {nn[1] * e1[2] - nn[2] * e1[1], nn[2] * e1[0] - nn[0] * e1[2],
+                          nn[0] * e1[1] - nn[1] * e1[0]};
+    for (int k = 0; k < 3; ++k) q[k] = e1[k], q[3 + k] = e2[k], q[6 + k] = nn[k];
+  }
+  const float cf[3] = {float(c[0]), float(c[1]), float(c[2])};
+  float qf[9];
+  for (int k = 0; k < 9; ++k) qf[k] = float(q[k]);
+  // pass 2: moments about the (FP32) centre in the cell frame
+  double M[35];
+#pragma unroll
+  for (int k = 0; k < 35; ++k) M[k] = 0.0;
+  double hmax = 0.0;
+  for (int b0 = 0; b0 < n; b0 += 128 * 32) {
+    float m[35];
+#pragma unroll
+    for (int k = 0; k < 35; ++k) m[k] = 0.f;
+    const int e = min(n, b0 + 128 * 32);
+    for (int i = b0 + t; i < e; i += 128) {
+      const float4 p = ys[s0 + i];
+      const float x0 = p.x - cf[0], x1 = p.y - cf[1], x2 = p.z - cf[2];
+      const float d0 = qf[0] * x0 + qf[1] * x1 + qf[2] * x2;
+      const float d1 = qf[3] * x0 + qf[4] * x1 + qf[5] * x2;
+      const float d2 = qf[6] * x0 + qf[7] * x1 + qf[8] * x2;
+      hmax = fmax(hmax, (double)sqrtf(d0 * d0 + d1 * d1 + d2 * d2));
+      float p0[5], p1[5], p2[5];
+      p0[0] = p1[0] = p2[0] = 1.f;
+#pragma unroll
+      for (int k = 1; k <= 4; ++k) p0[k] = p0[k - 1] * d0, p1[k] = p1[k - 1] * d1, p2[k] = p2[k - 1] * d2;
+      ff::sfor<35>([&](auto I) {
+        constexpr int k = decltype(I)::value;
+        m[k] = fmaf(p.w, p0[ff::mono_exp(k, 0)] * p1[ff::mono_exp(k, 1)] * p2[ff::mono_exp(k, 2)], m[k]);
+      });
+    }
+#pragma unroll
+    for (int k = 0; k < 35; ++k) M[k] += m[k];
+  }
+  block_sum128<35>(M, sh);
+  const double h = block_max128(hmax, sh);
+  if (t != 0) return;
+  float* r = cd + int64_t(cell) * kCellF;
+  for (int k = 0; k < kCellF; ++k) r[k] = 0.f;
+  r[0] = cf[0], r[1] = cf[1], r[2] = cf[2];
+  r[3] = float(cn);
+  r[4] = float(h);
+  r[5] = float(a[3]);
+  r[6] = float(a[4]);
+  r[7] = float(n);
+  for (int k = 0; k < 9; ++k) r[8 + k] = qf[k];
+  for (int k = 0; k < 35; ++k) r[kCellM + k] = float(M[k]);
+  // traced moments sum g d^b |d|^2 (|b| <= 2) and sum g |d|^4
+  for (int k = 0; k < 10; ++k) {
+    const int e0 = ff::mono_exp(k, 0), e1 = ff::mono_exp(k, 1), e2 = ff::mono_exp(k, 2);
+    r[kCellN1 + k] = float(M[ff::mono_index(e0 + 2, e1, e2)] + M[ff::mono_index(e0, e1 + 2, e2)] +
+                           M[ff::mono_index(e0, e1, e2 + 2)]);
+  }
+  {
+    double s4 = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        int e[3] = {0, 0, 0};
+        e[i] += 2;
+        e[j] += 2;
+        s4 += M[ff::mono_index(e[0], e[1], e[2])];
+      }
+    r[kCellN2] = float(s4);
+  }
+  // complex moments: z^p conj(z)^q w^k = sum over terms of u^a v^b w^k
+  const double S = a[3] > 0 ? a[3] : 1.0;
+  int j = 0;
+  for (int k = 0; k <= 4; ++k)
+    for (int nn = 0; nn <= 4 - k; ++nn)
+      for (int p = nn; 2 * p >= nn; --p) {
+        const int qq = nn - p;
+        // coefficients of (u + i v)^p (u - i v)^q over v powers
+        double cre[5] = {1, 0, 0, 0, 0}, cim[5] = {0, 0, 0, 0, 0};
+        int deg = 0;
+        for (int f = 0; f < p + qq; ++f) {
+          const double sg = f < p ? 1.0 : -1.0;  // multiply by (u + sg i v)
+          double nre[5] = {0, 0, 0, 0, 0}, nim[5] = {0, 0, 0, 0, 0};
+          for (int b = 0; b <= deg; ++b) {
+            nre[b] += cre[b];
+            nim[b] += cim[b];
+            nre[b + 1] += -sg * cim[b];
+            nim[b + 1] += sg * cre[b];
+          }
+          deg++;
+          for (int b = 0; b <= deg; ++b) cre[b] = nre[b], cim[b] = nim[b];
+        }
+        double re = 0, im = 0;
+        for (int b = 0; b <= nn; ++b) {
+          const double mv = M[ff::mono_index(nn - b, b, k)];
+          re += cre[b] * mv;
+          im += cim[b] * mv;
+        }
+        const double nrm = S * pow(h > 0 ? h : 1.0, double(nn + k));
+        r[kCellC + j] = float(re / nrm);
+        if (2 * p > nn) {
+          r[kCellC + j + 1] = float(im / nrm);
+          j += 2;
+        } else {
+          j += 1;
+        }
+      }
+}
+
+// One CTA (128 threads) per target block: Morton-ordered FP32 positions and
+// the block's bounding sphere.
+__global__ void __launch_bounds__(128) k_ff_tblocks(const double4* __restrict__ tgt,
+                                                    const int* __restrict__ tperm, int64_t ntgt,
+                                                    float4* __restrict__ xt, float4* __restrict__ box) {
+  __shared__ double sh[5 * 8];
+  const int64_t b = blockIdx.x;
+  const int t = threadIdx.x;
+  const int64_t i = b * kTargetBlock + t;
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (i < ntgt) {
+    const double4 p = tgt[tperm[i]];
+    x = make_float4(float(p.x), float(p.y), float(p.z), 1.f);
+  }
+  xt[i] = x;
+  double a[4] = {x.x, x.y, x.z, x.w};
+  block_sum128<4>(a, sh);
+  const float c0 = float(a[0] / a[3]), c1 = float(a[1] / a[3]), c2 = float(a[2] / a[3]);
+  double r = 0;
+  if (x.w > 0) {
+    const float e0 = x.x - c0, e1 = x.y - c1, e2 = x.z - c2;
+    r = sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+  }
+  r = block_max128(r, sh);
+  if (t == 0) box[b] = make_float4(c0, c1, c2, float(r) * (1.f + 1e-6f) + 1e-7f);
+}
+
+// One thread per target block: depth-first walk from the root.
+__global__ void k_ff_lists(const float* __restrict__ cd, const int4* __restrict__ cells,
+                           const float4* __restrict__ box, int64_t nblocks, float theta,
+                           float rho_min, int learn, int* __restrict__ far, int* __restrict__ near,
+                           int* __restrict__ lrn, int4* __restrict__ cnt) {
+  const int64_t b = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (b >= nblocks) return;
+  const float4 bx = box[b];
+  int stk[8 * 22];
+  int sp = 0;
+  stk[sp++] = 0;
+  int nf = 0, nn = 0, nl = 0, over = 0;
+  int* F = far + b * kFarCap;
+  int* N = near + b * kNearCap;
+  int* L = lrn + b * kLearnCap;
+  while (sp > 0) {
+    const int c = stk[--sp];
+    const float* r = cd + int64_t(c) * kCellF;
+    const float e0 = bx.x - r[0], e1 = bx.y - r[1], e2 = bx.z - r[2];
+    const float D = sqrtf(e0 * e0 + e1 * e1 + e2 * e2) - bx.w;
+    const float h = r[4];
+    const int4 ci = cells[c];
+    if (D > 0.f && h <= theta * D) {
+      if (nf < kFarCap) F[nf] = c;
+      nf++;
+      if (learn && h >= rho_min * D && ci.y >= 8) {
+        if (nl < kLearnCap) L[nl] = c;
+        nl++;
+      }
+    } else if (ci.w == 0) {
+      if (nn < kNearCap) N[nn] = c;
+      nn++;
+    } else {
+      if (sp + ci.w > 8 * 22) {
+        over = 1;
+        break;
+      }
+      for (int k = ci.w - 1; k >= 0; --k) stk[sp++] = ci.z + k;
+    }
+  }
+  if (nf > kFarCap || nn > kNearCap || nl > kLearnCap) over = 1;
+  cnt[b] = make_int4(min(nf, kFarCap), min(nn, kNearCap), min(nl, kLearnCap), over);
+}
+
+constexpr int kNearBuf = 512;
+constexpr int kFarBatch = 16;
+
+__device__ __forceinline__ void chord_acc(float x0, float x1, float x2, float4 s, float c0,
+                                          float& w0, float& w1, float& w2) {
+  const float d0 = x0 - s.x, d1 = x1 - s.y, d2 = x2 - s.z;
+  const float q = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, c0)));
+  const float r = s.w * rcp_approx(q);
+  w0 = fmaf(r, d0, w0);
+  w1 = fmaf(r, d1, w1);
+  w2 = fmaf(r, d2, w2);
+}
+
+// One CTA (128 threads, one target each) per target block.
+__global__ void __launch_bounds__(128) k_ff_eval(
+    const float4* __restrict__ xt, const int* __restrict__ tperm, int64_t ntgt,
+    const float4* __restrict__ ys, int64_t nsrc, const float* __restrict__ cd,
+    const int4* __restrict__ cells, const int* __restrict__ far, const int* __restrict__ near,
+    const int4* __restrict__ cnt, float c0, double* __restrict__ wout, int64_t wstride) {
+  __shared__ float4 buf[kNearBuf];
+  __shared__ float cell[kFarBatch][kCellF];
+  __shared__ int ofs[9];
+  const int64_t b = blockIdx.x;
+  const int t = threadIdx.x;
+  const float4 x = xt[b * kTargetBlock + t];
+  const int4 nc = cnt[b];
+  float S0 = 0.f, S1 = 0.f, S2 = 0.f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
+  if (nc.w) {
+    // lists overflowed: full direct sum (fallback)
+    for (int64_t j0 = 0; j0 < nsrc; j0 += kNearBuf) {
+      const int m = int(nsrc - j0 < kNearBuf ? nsrc - j0 : kNearBuf);
+      __syncthreads();
+      for (int i = t; i < m; i += 128) buf[i] = ys[j0 + i];
+      __syncthreads();
+      float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+      for (int i = 0; i < m; ++i) chord_acc(x.x, x.y, x.z, buf[i], c0, w0, w1, w2);
+      two_sum_acc(S0, C0, w0);
+      two_sum_acc(S1, C1, w1);
+      two_sum_acc(S2, C2, w2);
+    }
+  } else {
+    // near leaves, up to 8 per batch (<= 512 sources)
+    const int* N = near + b * kNearCap;
+    for (int l0 = 0; l0 < nc.y; l0 += 8) {
+      const int nl = min(8, nc.y - l0);
+      __syncthreads();
+      if (t == 0) {
+        int o = 0;
+        for (int k = 0; k < nl; ++k) {
+          ofs[k] = o;
+          o += min(cells[N[l0 + k]].y, kMaxLeaf);
+        }
+        ofs[nl] = o;
+      }
+      __syncthreads();
+      for (int k = 0; k < nl; ++k) {
+        const int4 ci = cells[N[l0 + k]];
+        const int m = ofs[k + 1] - ofs[k];
+        for (int i = t; i < m; i += 128) buf[ofs[k] + i] = ys[ci.x + i];
+      }
+      __syncthreads();
+      float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+      const int m = ofs[nl];
+      for (int i = 0; i < m; ++i) chord_acc(x.x, x.y, x.z, buf[i], c0, w0, w1, w2);
+      two_sum_acc(S0, C0, w0);
+      two_sum_acc(S1, C1, w1);
+      two_sum_acc(S2, C2, w2);
+      // leaves larger than kMaxLeaf (coincident points at the deepest level)
+      for (int k = 0; k < nl; ++k) {
+        const int4 ci = cells[N[l0 + k]];
+        if (ci.y <= kMaxLeaf) continue;
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+        for (int i = kMaxLeaf; i < ci.y; ++i) chord_acc(x.x, x.y, x.z, ys[ci.x + i], c0, v0, v1, v2);
+        two_sum_acc(S0, C0, v0);
+        two_sum_acc(S1, C1, v1);
+        two_sum_acc(S2, C2, v2);
+      }
+    }
+    // far cells: order-4 expansion, kFarBatch cells per batch
+    const int* F = far + b * kFarCap;
+    for (int f0 = 0; f0 < nc.x; f0 += kFarBatch) {
+      const int nb = min(kFarBatch, nc.x - f0);
+      __syncthreads();
+      for (int i = t; i < nb * kCellF; i += 128) {
+        const int k = i / kCellF, e = i - k * kCellF;
+        cell[k][e] = cd[int64_t(F[f0 + k]) * kCellF + e];
+      }
+      __syncthreads();
+      float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+      for (int k = 0; k < nb; ++k) {
+        float d[3], W[3], G[3];
+        ff::to_cell(cell[k], x.x, x.y, x.z, d);
+        ff::expand4(cell[k], d[0], d[1], d[2], c0, W);
+        ff::from_cell(cell[k], W, G);
+        w0 -= G[0];
+        w1 -= G[1];
+        w2 -= G[2];
+      }
+      two_sum_acc(S0, C0, w0);
+      two_sum_acc(S1, C1, w1);
+      two_sum_acc(S2, C2, w2);
+    }
+  }
+  const int64_t i = b * kTargetBlock + t;
+  if (i < ntgt && x.w > 0.f) {
+    const int64_t tt = tperm[i];
+    wout[tt] = double(S0) + double(C0);
+    wout[wstride + tt] = double(S1) + double(C1);
+    wout[2 * wstride + tt] = double(S2) + double(C2);
+  }
+}
+
+}  // namespace
+
+FFDevice::~FFDevice() {
+  for (void* p : allocs) cudaFree(p);
+}
+void* FFDevice::alloc(size_t bytes) {
+  void* p = nullptr;
+  LPM_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+  allocs.push_back(p);
+  return p;
+}
+
+void ff_cells(lpm_context& ctx, const float4* ys, const int4* cells, int ncells, float* cd) {
+  k_ff_cells<<<ncells, 128, 0, ctx.stream>>>(ys, cells, ncells, cd);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+void ff_launch_tree(lpm_context& ctx, FFDevice& d, const void* tgt, const void* src, double* wout,
+                    int64_t wstride, double c0, double theta, double rho_min, bool learn) {
+  cudaStream_t st = ctx.stream;
+  k_ff_sort_src<<<unsigned((d.nsrc + 255) / 256), 256, 0, st>>>(static_cast<const double4*>(src),
+                                                                 d.perm, d.nsrc, d.ys);
+  k_ff_cells<<<d.ncells, 128, 0, st>>>(d.ys, d.cells, d.ncells, d.cd);
+  k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4*>(tgt), d.tperm,
+                                                    d.ntgt, d.xt, d.box);
+  k_ff_lists<<<unsigned((d.nblocks + 63) / 64), 64, 0, st>>>(d.cd, d.cells, d.box, d.nblocks,
+                                                            float(theta), float(rho_min), learn,
+                                                            d.far, d.near, d.lrn, d.cnt);
+  k_ff_eval<<<unsigned(d.nblocks), 128, 0, st>>>(d.xt, d.tperm, d.ntgt, d.ys, d.nsrc, d.cd,
+                                                 d.cells, d.far, d.near, d.cnt, float(c0), wout,
+                                                 wstride);
+  ctx.launches += 5;
+  LPM_CUDA(cudaGetLastError());
+}
+
+}  // namespace lpm
+
+// ---------------------------------------------------------------------------
+// lpm_farfield host methods
+// ---------------------------------------------------------------------------
+lpm_farfield::~lpm_farfield() { delete d; }
+
+bool lpm_farfield::built() const { return d != nullptr && d->ncells > 0; }
+
+void lpm_farfield::build(const double* src_xyz, int64_t nsrc, const double* tgt_xyz, int64_t ntgt) {
+  using namespace lpm;
+  TreeTopo tp = build_tree(src_xyz, nsrc, tgt_xyz, ntgt, leaf_max);
+  ff_prepare_kernels();
+  FFDevice* nd = new FFDevice();
+  try {
+    nd->nsrc = nsrc;
+    nd->ntgt = ntgt;
+    nd->ncells = int(tp.start.size());
+    nd->nblocks = (ntgt + kTargetBlock - 1) / kTargetBlock;
+    nd->perm = static_cast<int*>(nd->alloc(sizeof(int) * nsrc));
+    nd->tperm = static_cast<int*>(nd->alloc(sizeof(int) * std::max<int64_t>(ntgt, 1)));
+    nd->cells = static_cast<int4*>(nd->alloc(sizeof(int4) * nd->ncells));
+    nd->ys = static_cast<float4*>(nd->alloc(sizeof(float4) * nsrc));
+    nd->cd = static_cast<float*>(nd->alloc(sizeof(float) * kCellF * size_t(nd->ncells)));
+    nd->xt = static_cast<float4*>(nd->alloc(sizeof(float4) * kTargetBlock * size_t(nd->nblocks)));
+    nd->box = static_cast<float4*>(nd->alloc(sizeof(float4) * size_t(nd->nblocks)));
+    nd->far = static_cast<int*>(nd->alloc(sizeof(int) * kFarCap * size_t(nd->nblocks)));
+    nd->near = static_cast<int*>(nd->alloc(sizeof(int) * kNearCap * size_t(nd->nblocks)));
+    nd->lrn = static_cast<int*>(nd->alloc(sizeof(int) * kLearnCap * size_t(nd->nblocks)));
+    nd->cnt = static_cast<int4*>(nd->alloc(sizeof(int4) * size_t(nd->nblocks)));
+    nd->counter = static_cast<int*>(nd->alloc(sizeof(int) * 4));
+    std::vector<int4> ci(nd->ncells);
+    for (int i = 0; i < nd->ncells; ++i) ci[i] = make_int4(tp.start[i], tp.count[i], tp.child0[i], tp.nchild[i]);
+    cudaStream_t st = ctx->stream;
+    LPM_CUDA(cudaMemcpyAsync(nd->perm, tp.perm.data(), sizeof(int) * nsrc, cudaMemcpyHostToDevice, st));
+    if (ntgt > 0)
+      LPM_CUDA(cudaMemcpyAsync(nd->tperm, tp.tperm.data(), sizeof(int) * ntgt, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaMemcpyAsync(nd->cells, ci.data(), sizeof(int4) * nd->ncells, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    delete nd;
+    throw;
+  }
+  delete d;
+  d = nd;
+}
+
+void lpm_farfield::evaluate(const void* tgt, const void* src, double* wout, int64_t wstride,
+                            double c0, double eps) {
+  using namespace lpm;
+  if (!built()) throw Error(LPM_ERR_STATE, "far field: tree not built");
+  const bool learn = use_net && trained;
+  ff_launch_tree(*ctx, *d, tgt, src, wout, wstride, c0, theta, rho_min, learn);
+  if (learn) ff_launch_mlp(*ctx, *d, *net, wout, wstride, eps, rho_min);
+}
+
+void lpm_farfield::counts() {
+  using namespace lpm;
+  std::vector<int4> c(d->nblocks);
+  LPM_CUDA(cudaMemcpyAsync(c.data(), d->cnt, sizeof(int4) * d->nblocks, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  LPM_CUDA(cudaStreamSynchronize(ctx->stream));
+  last_far = last_near = last_learn = last_fallback = 0;
+  std::vector<int4> cells(d->ncells);
+  LPM_CUDA(cudaMemcpy(cells.data(), d->cells, sizeof(int4) * d->ncells, cudaMemcpyDeviceToHost));
+  std::vector<int> nearl(size_t(d->nblocks) * kNearCap);
+  LPM_CUDA(cudaMemcpy(nearl.data(), d->near, sizeof(int) * nearl.size(), cudaMemcpyDeviceToHost));
+  for (int64_t b = 0; b < d->nblocks; ++b) {
+    if (c[b].w) {
+      last_fallback++;
+      continue;
+    }
+    last_far += c[b].x;
+    last_learn += c[b].z;
+    for (int k = 0; k < c[b].y; ++k) last_near += cells[nearl[b * kNearCap + k]].y;
+  }
+}

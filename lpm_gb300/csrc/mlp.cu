@@ -1,0 +1,1046 @@
+// mlp.cu -- learned far-field correction on the fifth-generation tensor cores.
+//
+// The network maps the features of one (target, far cell) pair -- the cell's
+// complex moments to order 4 rotated into the target's canonical frame, the
+// target offset, h/D, eps/D and h -- to the residual of the order-4 expansion
+// (canonical frame, normalised by S rho^5 / (2 pi D)).  48 -> 128 -> 128 ->
+// 128 -> 16, SiLU, BF16 weights and activations, FP32 accumulation in TMEM.
+//
+// Tile = 128 rows (one target block against one cell at inference, 128
+// training samples in training) x one layer: tcgen05.mma with M = 128,
+// N = 128 (16 for the output layer), K = 16 per instruction, operands in
+// shared memory (layout in tc.cuh), accumulator in TMEM; one thread issues,
+// tcgen05.commit arrives on an mbarrier, the 4 warps read their 32 TMEM lanes
+// back (tcgen05.ld), apply bias/SiLU and write the next layer's BF16 operand.
+//
+// Training (k_mlp_train): one tile per CTA, forward then backward in the
+// same CTA with every GEMM on the tensor cores:
+//   dW4^T = A3^T dY        (M 128, N 16, K = 128 rows; MN-major A and B)
+//   dA3   = dY W4          (K = 16; K-major A, MN-major B)
+//   Z3    = A2 W3^T        (recomputed instead of stored)
+//   dZ3   = dA3 * silu'(Z3), written over A3
+//   dW3   = dZ3^T A2, dA2 = dZ3 W3, Z2 = A1 W2^T, ... down to dW1 = dZ1^T X.
+// TMEM: 512 columns = work (Z, dA) | recomputed Z | gradient | spare.
+// Per-CTA gradients go to a partial buffer that k_mlp_adam reduces in fixed
+// order (deterministic) before the Adam update, which also rewrites the BF16
+// tile-layout copy the kernels load.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "farfield_dev.cuh"
+#include "ffmath.cuh"
+#include "nbody.cuh"
+#include "tc.cuh"
+
+namespace lpm {
+
+namespace {
+
+// shared-memory map (bytes)
+constexpr int kSmW1 = 0;
+constexpr int kSmW2 = kSmW1 + kHid * kIn * 2;
+constexpr int kSmW3 = kSmW2 + kHid * kHid * 2;
+constexpr int kSmW4 = kSmW3 + kHid * kHid * 2;
+constexpr int kSmWEnd = kSmW4 + kOut * kHid * 2;  // 81920
+constexpr int kSmX = kSmWEnd;
+constexpr int kSmA1 = kSmX + 128 * kIn * 2;
+constexpr int kSmA2 = kSmA1 + 128 * kHid * 2;
+constexpr int kSmA3 = kSmA2 + 128 * kHid * 2;
+constexpr int kSmDY = kSmA3 + 128 * kHid * 2;
+constexpr int kSmTrain = kSmDY + 128 * kOut * 2;  // 196608
+constexpr int kSmInfCell = kSmA2;                 // inference: X, H = A1, cell record
+constexpr int kSmInfer = kSmInfCell + kCellF * 4 + 512;
+
+// element offsets of the matrices in the BF16 weight image and the FP32
+// master vector (same order)
+constexpr int kO1 = 0, kO2 = kW1, kO3 = kW1 + kW2, kO4 = kW1 + kW2 + kW3;
+
+constexpr uint32_t kID128 = tc::idesc_bf16(128, 128, false, false);
+constexpr uint32_t kID16 = tc::idesc_bf16(128, 16, false, false);
+
+__device__ __forceinline__ uint32_t sbase(const unsigned char* sm, int off) {
+  return smem_u32(sm + off);
+}
+
+// D (tmem) = A (rows x K, K-major) * B^T (N x K, K-major), K = 16 * ksteps
+__device__ __forceinline__ void gemm_kk(uint32_t d, uint32_t a, uint32_t asbo, uint32_t b,
+                                        uint32_t bsbo, uint32_t id, int ksteps) {
+  for (int s = 0; s < ksteps; ++s)
+    tc::mma_bf16(d, tc::sdesc(a + 256 * s, 128, asbo), tc::sdesc(b + 256 * s, 128, bsbo), id,
+                 s > 0);  // K-major A and B
+}
+
+// Waits for the commit of phase `ph`; false if it did not arrive in time.
+__device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
+  const bool ok = mbar_wait_bounded(bar, ph);
+  ph ^= 1u;
+  tc::fence_after();
+  return ok;
+}
+
+// Bias + SiLU epilogue of one 128-column layer: TMEM lane row -> BF16 row of
+// the next operand (unit kBiasHid is the constant 1).
+__device__ __forceinline__ void silu_rows(uint32_t tacc, int warp, unsigned char* dst, int row) {
+#pragma unroll 1
+  for (int cc = 0; cc < kHid; cc += 16) {
+    float v[16];
+    tc::ld16(tc::lane_addr(tacc, warp, cc), v);
+    uint32_t p[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float a = ff::silu(v[2 * i]), b = ff::silu(v[2 * i + 1]);
+      if (cc + 2 * i + 1 == kBiasHid) b = 1.f;
+      p[i] = tc::pack_bf16(a, b);
+    }
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc, kHid)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);
+  }
+}
+
+// Backward epilogue: dZ = dA * silu'(Z) (unit kBiasHid carries no gradient).
+__device__ __forceinline__ void dsilu_rows(uint32_t tda, uint32_t tz, int warp, unsigned char* dst,
+                                           int row) {
+#pragma unroll 1
+  for (int cc = 0; cc < kHid; cc += 16) {
+    float a[16], z[16];
+    tc::ld16(tc::lane_addr(tda, warp, cc), a);
+    tc::ld16(tc::lane_addr(tz, warp, cc), z);
+    uint32_t p[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float x = a[2 * i] * ff::silu_grad(z[2 * i]);
+      float y = a[2 * i + 1] * ff::silu_grad(z[2 * i + 1]);
+      if (cc + 2 * i + 1 == kBiasHid) y = 0.f;
+      p[i] = tc::pack_bf16(x, y);
+    }
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc, kHid)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);
+  }
+}
+
+__device__ __forceinline__ void write_x_row(unsigned char* sm, int row, const float* f) {
+#pragma unroll
+  for (int j = 0; j < kIn / 8; ++j) {
+    uint4 u = make_uint4(tc::pack_bf16(f[8 * j], f[8 * j + 1]), tc::pack_bf16(f[8 * j + 2], f[8 * j + 3]),
+                         tc::pack_bf16(f[8 * j + 4], f[8 * j + 5]), tc::pack_bf16(f[8 * j + 6], f[8 * j + 7]));
+    *reinterpret_cast<uint4*>(sm + kSmX + tc::cm_off(row, 8 * j, kIn)) = u;
+  }
+}
+
+__device__ __forceinline__ void load_weights(unsigned char* sm, const uint16_t* wbf) {
+  const uint4* s = reinterpret_cast<const uint4*>(wbf);
+  uint4* d = reinterpret_cast<uint4*>(sm);
+  for (int i = threadIdx.x; i < kSmWEnd / 16; i += blockDim.x) d[i] = s[i];
+}
+
+// Forward through layers 1-3 for the X tile; activations into a1/a2/a3
+// (inference passes the same buffer three times).  Returns false on a timed
+// out wait (all threads agree).
+__device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t* bar, uint32_t& ph,
+                                        int a1, int a2, int a3) {
+  const int t = threadIdx.x, w = t >> 5;
+  const int in_buf[3] = {kSmX, a1, a2};
+  const int out_buf[3] = {a1, a2, a3};
+  const int wts[3] = {kSmW1, kSmW2, kSmW3};
+#pragma unroll 1
+  for (int l = 0; l < 3; ++l) {
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after();
+      const int k = l == 0 ? kIn : kHid;
+      gemm_kk(tb, sbase(sm, in_buf[l]), k * 16, sbase(sm, wts[l]), k * 16, kID128, k / 16);
+      tc::commit(bar);
+    }
+    const bool ok = wait_mma(bar, ph);
+    if (__syncthreads_or(!ok)) return false;
+    silu_rows(tb, w, sm + out_buf[l], t);
+  }
+  // output layer (N = 16) into columns 0..15
+  tc::fence_smem_async();
+  tc::fence_before();
+  __syncthreads();
+  if (t == 0) {
+    tc::fence_after();
+    gemm_kk(tb, sbase(sm, a3), kHid * 16, sbase(sm, kSmW4), kHid * 16, kID16, kHid / 16);
+    tc::commit(bar);
+  }
+  const bool ok = wait_mma(bar, ph);
+  return !__syncthreads_or(!ok);
+}
+
+struct MlpArgs {
+  const float4* xt;
+  const int* tperm;
+  int64_t ntgt, nblocks;
+  const float* cd;
+  const int* lrn;
+  const int4* cnt;
+  const uint16_t* wbf;
+  const float* norm;
+  double* wout;
+  int64_t wstride;
+  float eps, rho_min;
+  int* counter;
+  int* err;
+};
+
+// Persistent: one CTA per SM pulls target blocks; per block, one tile per
+// learned cell; the correction is accumulated per target in registers.
+__global__ void __launch_bounds__(128, 1) k_ff_mlp(const MlpArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  __shared__ int blk;
+  __shared__ float nrm[2 * kIn + 1];
+  const int t = threadIdx.x, w = t >> 5;
+  load_weights(sm, a.wbf);
+  for (int i = t; i < 2 * kIn + 1; i += 128) nrm[i] = a.norm[i];
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  if (w == 0) tc::tmem_alloc(&tslot, 128);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tb = tslot;
+  uint32_t ph = 0;
+  bool ok = true;
+  float* cell = reinterpret_cast<float*>(sm + kSmInfCell);
+  const float oscale = nrm[2 * kIn];
+  for (;;) {
+    __syncthreads();
+    if (t == 0) blk = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int64_t b = blk;
+    if (b >= a.nblocks) break;
+    const int4 nc = a.cnt[b];
+    if (nc.w || nc.z == 0) continue;
+    const float4 x = a.xt[b * kTargetBlock + t];
+    float acc[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < nc.z && ok; ++k) {
+      const int c = a.lrn[b * kLearnCap + k];
+      __syncthreads();
+      for (int i = t; i < kCellF; i += 128) cell[i] = a.cd[int64_t(c) * kCellF + i];
+      __syncthreads();
+      float d[3];
+      ff::to_cell(cell, x.x, x.y, x.z, d);
+      const ff::PairGeo g = ff::pair_geo(cell, d);
+      const bool use = x.w > 0.f && g.rho >= a.rho_min && g.rho <= 1.f;
+      float f[kIn];
+      ff::pair_features(cell, g, a.eps, f);
+      f[kBiasIn] = 1.f;
+#pragma unroll
+      for (int i = kBiasIn + 1; i < kIn; ++i) f[i] = 0.f;
+#pragma unroll
+      for (int i = 0; i < kIn; ++i) f[i] = (f[i] - nrm[i]) * nrm[kIn + i];
+      write_x_row(sm, t, f);
+      ok = forward(sm, tb, &bar, ph, kSmA1, kSmA1, kSmA1);
+      if (!ok) break;
+      float o[16];
+      tc::ld16(tc::lane_addr(tb, w, 0), o);
+      if (use) {
+        float dw[3];
+        ff::correction(cell, g, o, oscale, x.x, x.y, x.z, dw);
+        acc[0] += dw[0];
+        acc[1] += dw[1];
+        acc[2] += dw[2];
+      }
+    }
+    if (!ok) break;
+    const int64_t i = b * kTargetBlock + t;
+    if (i < a.ntgt && x.w > 0.f) {
+      const int64_t tt = a.tperm[i];
+      a.wout[tt] += acc[0];
+      a.wout[a.wstride + tt] += acc[1];
+      a.wout[2 * a.wstride + tt] += acc[2];
+    }
+  }
+  if (!ok && t == 0) atomicExch(a.err, 1);
+  tc::fence_before();
+  __syncthreads();
+  if (w == 0) tc::tmem_dealloc(tb, 128);
+}
+
+// ---------------------------------------------------------------------------
+// Training samples
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double unif(uint64_t h) { return double(h >> 11) * (1.0 / 9007199254740992.0); }
+
+// One CTA (128 threads) per job (cell, tile): 128 random targets on the unit
+// sphere with h/|x - c| uniform in [rho_min, theta]; the exact FP64 chord
+// sum over the cell's points minus the FP32 order-4 expansion is the
+// residual velocity, stored in the target's canonical frame and normalised.
+__global__ void __launch_bounds__(128) k_ff_samples(const float* __restrict__ cd,
+                                                    const int4* __restrict__ cells,
+                                                    const double4* __restrict__ ysd,
+                                                    const int* __restrict__ jobs, int njobs,
+                                                    uint64_t seed, float theta, float rho_min,
+                                                    float eps, double c0, float* __restrict__ X,
+                                                    float* __restrict__ Y, int64_t row0,
+                                                    int64_t nrows) {
+  __shared__ double4 buf[256];
+  const int job = blockIdx.x;
+  const int t = threadIdx.x;
+  const int c = jobs[job];
+  const float* cell = cd + int64_t(c) * kCellF;
+  const int4 ci = cells[c];
+  const uint64_t h0 = mix64(seed ^ mix64(uint64_t(job) * 131 + t));
+  const double u1 = unif(h0), u2 = unif(mix64(h0));
+  const double h = cell[4], cn = cell[3];
+  const double rho = rho_min + (theta - rho_min) * u1;
+  const double D = h / rho;
+  double ca = cn > 0 ? (1.0 + cn * cn - D * D) / (2.0 * cn) : 0.0;
+  ca = fmin(1.0, fmax(-1.0, ca));
+  const double sa = sqrt(fmax(0.0, 1.0 - ca * ca));
+  const double be = 6.283185307179586 * u2;
+  double x[3];
+  for (int k = 0; k < 3; ++k)
+    x[k] = ca * cell[14 + k] + sa * (cos(be) * cell[8 + k] + sin(be) * cell[11 + k]);
+  const double xn = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  for (int k = 0; k < 3; ++k) x[k] /= xn;
+  double we[3] = {0, 0, 0};
+  for (int j0 = 0; j0 < ci.y; j0 += 256) {
+    const int m = min(256, ci.y - j0);
+    __syncthreads();
+    for (int i = t; i < m; i += 128) buf[i] = ysd[ci.x + j0 + i];
+    __syncthreads();
+    for (int i = 0; i < m; ++i) {
+      const double4 s = buf[i];
+      const double d0 = x[0] - s.x, d1 = x[1] - s.y, d2 = x[2] - s.z;
+      const double r = s.w / (d0 * d0 + d1 * d1 + d2 * d2 + c0);
+      we[0] += r * d0;
+      we[1] += r * d1;
+      we[2] += r * d2;
+    }
+  }
+  const float xf[3] = {float(x[0]), float(x[1]), float(x[2])};
+  float d[3], Wc[3], W[3];
+  ff::to_cell(cell, xf[0], xf[1], xf[2], d);
+  ff::expand4(cell, d[0], d[1], d[2], float(c0), Wc);
+  ff::from_cell(cell, Wc, W);
+  // u = -(1/2pi) w cross x with w_exact = we, w_expansion = -W
+  const double ip = 1.0 / 6.283185307179586;
+  double R[3];
+  {
+    const double wd[3] = {we[0] + W[0], we[1] + W[1], we[2] + W[2]};
+    R[0] = -ip * (wd[1] * x[2] - wd[2] * x[1]);
+    R[1] = -ip * (wd[2] * x[0] - wd[0] * x[2]);
+    R[2] = -ip * (wd[0] * x[1] - wd[1] * x[0]);
+  }
+  const ff::PairGeo g = ff::pair_geo(cell, d);
+  float f[kIn];
+  ff::pair_features(cell, g, eps, f);
+  f[kBiasIn] = 1.f;
+  for (int i = kBiasIn + 1; i < kIn; ++i) f[i] = 0.f;
+  const int64_t row = row0 + int64_t(job) * 128 + t;
+  if (row >= nrows) return;
+  for (int i = 0; i < kIn; ++i) X[row * kIn + i] = f[i];
+  // canonical frame: e1' = cs e1 + sn e2, e2' = -sn e1 + cs e2, n
+  double e1[3], e2[3];
+  for (int k = 0; k < 3; ++k) {
+    e1[k] = g.cs * cell[8 + k] + g.sn * cell[11 + k];
+    e2[k] = -g.sn * cell[8 + k] + g.cs * cell[11 + k];
+  }
+  const double is = g.scale > 0 ? 1.0 / g.scale : 0.0;
+  Y[row * 4 + 0] = float((R[0] * e1[0] + R[1] * e1[1] + R[2] * e1[2]) * is);
+  Y[row * 4 + 1] = float((R[0] * e2[0] + R[1] * e2[1] + R[2] * e2[2]) * is);
+  Y[row * 4 + 2] = float((R[0] * cell[14] + R[1] * cell[15] + R[2] * cell[16]) * is);
+  Y[row * 4 + 3] = 0.f;
+}
+
+// Per-feature sums and sums of squares (FP64, fixed-order per block) and
+// the sum of squared targets; partial[blk][2*kIn + 1].
+__global__ void __launch_bounds__(256) k_ff_stats(const float* __restrict__ X, const float* __restrict__ Y,
+                                                  int64_t n, double* __restrict__ part) {
+  __shared__ double sh[256];
+  const int t = threadIdx.x;
+  for (int f = 0; f <= 2 * kIn; ++f) {
+    double s = 0;
+    for (int64_t r = blockIdx.x * int64_t(256) + t; r < n; r += int64_t(gridDim.x) * 256) {
+      if (f < kIn) {
+        s += X[r * kIn + f];
+      } else if (f < 2 * kIn) {
+        const double v = X[r * kIn + f - kIn];
+        s += v * v;
+      } else {
+        const double a = Y[r * 4], b = Y[r * 4 + 1], c = Y[r * 4 + 2];
+        s += a * a + b * b + c * c;
+      }
+    }
+    sh[t] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+      if (t < o) sh[t] += sh[t + o];
+      __syncthreads();
+    }
+    if (t == 0) part[blockIdx.x * (2 * kIn + 1) + f] = sh[0];
+    __syncthreads();
+  }
+}
+
+__global__ void k_ff_normalise(const float* __restrict__ X, const float* __restrict__ Y, int64_t n,
+                               const float* __restrict__ norm, uint16_t* __restrict__ Xb,
+                               float* __restrict__ Yn) {
+  const int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (r >= n) return;
+  for (int f = 0; f < kIn; f += 2) {
+    const float a = (X[r * kIn + f] - norm[f]) * norm[kIn + f];
+    const float b = (X[r * kIn + f + 1] - norm[f + 1]) * norm[kIn + f + 1];
+    reinterpret_cast<uint32_t*>(Xb + r * kIn)[f / 2] = tc::pack_bf16(a, b);
+  }
+  const float is = norm[2 * kIn] > 0 ? 1.f / norm[2 * kIn] : 0.f;
+  for (int k = 0; k < 4; ++k) Yn[r * 4 + k] = Y[r * 4 + k] * is;
+}
+
+// ---------------------------------------------------------------------------
+// Training step
+// ---------------------------------------------------------------------------
+struct TrainArgs {
+  const uint16_t* Xb;  // n x 48 BF16 (normalised)
+  const float* Yn;     // n x 4 (normalised targets)
+  int64_t n;
+  uint64_t pa, pb;     // sample of row i: (pa * i + pb) mod n
+  int64_t row0;
+  float inv_batch;
+  const uint16_t* wbf;
+  float* gpart;        // per CTA: kNParam gradients
+  float* lpart;        // per CTA: sum of squared errors
+  int* err;
+};
+
+__global__ void __launch_bounds__(128, 1) k_mlp_train(const TrainArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  __shared__ float red[4];
+  const int t = threadIdx.x, w = t >> 5;
+  load_weights(sm, a.wbf);
+  const uint64_t i = uint64_t(a.row0) + uint64_t(blockIdx.x) * 128 + t;
+  const int64_t r = int64_t((a.pa * i + a.pb) % uint64_t(a.n));
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(a.Xb + r * kIn);
+#pragma unroll
+    for (int j = 0; j < kIn / 8; ++j)
+      *reinterpret_cast<uint4*>(sm + kSmX + tc::cm_off(t, 8 * j, kIn)) = src[j];
+  }
+  const float y0 = a.Yn[r * 4], y1 = a.Yn[r * 4 + 1], y2 = a.Yn[r * 4 + 2];
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  if (w == 0) tc::tmem_alloc(&tslot, 512);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tb = tslot, T0 = tb, T1 = tb + 128, T2 = tb + 256;
+  uint32_t ph = 0;
+  bool ok = forward(sm, tb, &bar, ph, kSmA1, kSmA2, kSmA3);
+  float* g = a.gpart + int64_t(blockIdx.x) * kNParam;
+  float loss = 0.f;
+  if (ok) {
+    float o[16];
+    tc::ld16(tc::lane_addr(T0, w, 0), o);
+    const float e0 = o[0] - y0, e1 = o[1] - y1, e2 = o[2] - y2;
+    loss = e0 * e0 + e1 * e1 + e2 * e2;
+    const float k = 2.f * a.inv_batch;
+    const uint4 u = make_uint4(tc::pack_bf16(k * e0, k * e1), tc::pack_bf16(k * e2, 0.f), 0u, 0u);
+    *reinterpret_cast<uint4*>(sm + kSmDY + tc::cm_off(t, 0, kOut)) = u;
+    *reinterpret_cast<uint4*>(sm + kSmDY + tc::cm_off(t, 8, kOut)) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  // backward: three hidden layers, l = 3, 2, 1
+  const int Abuf[4] = {kSmX, kSmA1, kSmA2, kSmA3};
+  const int Wbuf[4] = {0, kSmW1, kSmW2, kSmW3};
+  const int Goff[4] = {0, kO1, kO2, kO3};
+#pragma unroll 1
+  for (int l = 3; l >= 1 && ok; --l) {
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after();
+      if (l == 3) {
+        // dW4^T = A3^T dY ; dA3 = dY W4
+        for (int s = 0; s < 8; ++s)
+          tc::mma_bf16(T2, tc::sdesc_mn(sbase(sm, kSmA3) + s * 2 * kHid * 16, kHid),
+                       tc::sdesc_mn(sbase(sm, kSmDY) + s * 2 * kOut * 16, kOut),
+                       tc::idesc_bf16(128, 16, true, true), s > 0);
+        tc::mma_bf16(T0, tc::sdesc_k(sbase(sm, kSmDY), kOut), tc::sdesc_mn(sbase(sm, kSmW4), kHid),
+                     tc::idesc_bf16(128, 128, false, true), 0);
+      } else {
+        // dW_(l+1) = dZ_(l+1)^T A_l ; dA_l = dZ_(l+1) W_(l+1)   (dZ_(l+1) over A_(l+1))
+        const int dz = Abuf[l + 1];
+        for (int s = 0; s < 8; ++s)
+          tc::mma_bf16(T2, tc::sdesc_mn(sbase(sm, dz) + s * 2 * kHid * 16, kHid),
+                       tc::sdesc_mn(sbase(sm, Abuf[l]) + s * 2 * kHid * 16, kHid),
+                       tc::idesc_bf16(128, 128, true, true), s > 0);
+        for (int s = 0; s < 8; ++s)
+          tc::mma_bf16(T0, tc::sdesc_k(sbase(sm, dz) + s * 256, kHid),
+                       tc::sdesc_mn(sbase(sm, Wbuf[l + 1]) + s * 2 * kHid * 16, kHid),
+                       tc::idesc_bf16(128, 128, false, true), s > 0);
+      }
+      // recompute Z_l = A_(l-1) W_l^T
+      const int k = l == 1 ? kIn : kHid;
+      gemm_kk(T1, sbase(sm, Abuf[l - 1]), k * 16, sbase(sm, Wbuf[l]), k * 16, kID128, k / 16);
+      tc::commit(&bar);
+    }
+    ok = wait_mma(&bar, ph);
+    if (__syncthreads_or(!ok)) {
+      ok = false;
+      break;
+    }
+    // gradient of the layer above
+    if (l == 3) {
+      float v[16];
+      tc::ld16(tc::lane_addr(T2, w, 0), v);
+#pragma unroll
+      for (int o = 0; o < kOut; ++o) g[kO4 + o * kHid + t] = v[o];
+    } else {
+      float* gr = g + Goff[l + 1] + t * kHid;
+#pragma unroll 1
+      for (int cc = 0; cc < kHid; cc += 16) {
+        float v[16];
+        tc::ld16(tc::lane_addr(T2, w, cc), v);
+#pragma unroll
+        for (int q = 0; q < 16; q += 4)
+          *reinterpret_cast<float4*>(gr + cc + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+      }
+    }
+    // dZ_l over A_l
+    dsilu_rows(T0, T1, w, sm + Abuf[l], t);
+  }
+  if (ok) {
+    // dW1 = dZ1^T X  (N = 48)
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    if (t == 0) {
+      tc::fence_after();
+      for (int s = 0; s < 8; ++s)
+        tc::mma_bf16(T2, tc::sdesc_mn(sbase(sm, kSmA1) + s * 2 * kHid * 16, kHid),
+                     tc::sdesc_mn(sbase(sm, kSmX) + s * 2 * kIn * 16, kIn),
+                     tc::idesc_bf16(128, kIn, true, true), s > 0);
+      tc::commit(&bar);
+    }
+    ok = wait_mma(&bar, ph);
+    if (__syncthreads_or(!ok)) ok = false;
+    if (ok) {
+      float* gr = g + kO1 + t * kIn;
+#pragma unroll 1
+      for (int cc = 0; cc < kIn; cc += 16) {
+        float v[16];
+        tc::ld16(tc::lane_addr(T2, w, cc), v);
+#pragma unroll
+        for (int q = 0; q < 16; q += 4)
+          *reinterpret_cast<float4*>(gr + cc + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+      }
+    }
+  }
+  // loss of the tile (fixed order)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_down_sync(0xffffffffu, loss, o);
+  if ((t & 31) == 0) red[w] = loss;
+  tc::fence_before();
+  __syncthreads();
+  if (t == 0) {
+    a.lpart[blockIdx.x] = (red[0] + red[1]) + (red[2] + red[3]);
+    if (!ok) atomicExch(a.err, 1);
+  }
+  if (w == 0) tc::tmem_dealloc(tb, 512);
+}
+
+__device__ __forceinline__ int wimage_offset(int i) {
+  // master index -> element offset in the BF16 tile image
+  if (i < kO2) return kO1 + int(tc::cm_off(i / kIn, i % kIn, kIn) / 2);
+  if (i < kO3) return kO2 + int(tc::cm_off((i - kO2) / kHid, (i - kO2) % kHid, kHid) / 2);
+  if (i < kO4) return kO3 + int(tc::cm_off((i - kO3) / kHid, (i - kO3) % kHid, kHid) / 2);
+  return kO4 + int(tc::cm_off((i - kO4) / kHid, (i - kO4) % kHid, kHid) / 2);
+}
+
+// Fixed-order reduction of the per-CTA gradients, Adam update, BF16 image.
+__global__ void k_mlp_adam(const float* __restrict__ gpart, int nparts, float* __restrict__ wm,
+                           float* __restrict__ m, float* __restrict__ v, uint16_t* __restrict__ wbf,
+                           float lr, float b1, float b2, float bc1, float bc2, float aeps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kNParam) return;
+  float gsum = 0.f;
+  for (int p = 0; p < nparts; ++p) gsum += gpart[int64_t(p) * kNParam + i];
+  const float mi = b1 * m[i] + (1.f - b1) * gsum;
+  const float vi = b2 * v[i] + (1.f - b2) * gsum * gsum;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = wm[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + aeps);
+  wm[i] = wi;
+  __nv_bfloat16 hb = __float2bfloat16(wi);
+  wbf[wimage_offset(i)] = *reinterpret_cast<uint16_t*>(&hb);
+}
+
+__global__ void k_mlp_image(const float* __restrict__ wm, uint16_t* __restrict__ wbf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kNParam) return;
+  __nv_bfloat16 hb = __float2bfloat16(wm[i]);
+  wbf[wimage_offset(i)] = *reinterpret_cast<uint16_t*>(&hb);
+}
+
+// Self-test of the operand layouts: D (128 x N) = A * B with A given as
+// 128 x K (K-major) or K x 128 (MN-major) and B as N x K (K-major) or K x N
+// (MN-major), all row-major FP32 in global memory, rounded to BF16.
+constexpr int kSelfBuf = 32768;
+__global__ void __launch_bounds__(128) k_tc_selftest(const float* A, const float* B, float* D,
+                                                     int N, int K, int amn, int bmn, int* err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  const int t = threadIdx.x, w = t >> 5;
+  unsigned char* sa = sm;
+  unsigned char* sb = sm + kSelfBuf;
+  const int ar = amn ? K : 128, ac = amn ? 128 : K, br = bmn ? K : N, bc = bmn ? N : K;
+  for (int i = t; i < ar * ac; i += 128) {
+    __nv_bfloat16 h = __float2bfloat16(A[i]);
+    *reinterpret_cast<__nv_bfloat16*>(sa + tc::cm_off(i / ac, i % ac, ac)) = h;
+  }
+  for (int i = t; i < br * bc; i += 128) {
+    __nv_bfloat16 h = __float2bfloat16(B[i]);
+    *reinterpret_cast<__nv_bfloat16*>(sb + tc::cm_off(i / bc, i % bc, bc)) = h;
+  }
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  tc::fence_smem_async();
+  if (w == 0) tc::tmem_alloc(&tslot, 128);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tb = tslot;
+  if (t == 0) {
+    for (int s = 0; s < K / 16; ++s) {
+      const uint64_t da = amn ? tc::sdesc_mn(smem_u32(sa) + s * 2 * ac * 16, ac)
+                              : tc::sdesc_k(smem_u32(sa) + s * 256, ac);
+      const uint64_t db = bmn ? tc::sdesc_mn(smem_u32(sb) + s * 2 * bc * 16, bc)
+                              : tc::sdesc_k(smem_u32(sb) + s * 256, bc);
+      tc::mma_bf16(tb, da, db, tc::idesc_bf16(128, N, amn != 0, bmn != 0), s > 0);
+    }
+    tc::commit(&bar);
+  }
+  uint32_t ph = 0;
+  const bool ok = wait_mma(&bar, ph);
+  if (!ok) {
+    if (t == 0) atomicExch(err, 1);
+  } else {
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      tc::ld16(tc::lane_addr(tb, w, c), v);
+      for (int j = 0; j < 16; ++j) D[t * N + c + j] = v[j];
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (w == 0) tc::tmem_dealloc(tb, 128);
+}
+
+}  // namespace
+
+FFNet::~FFNet() {
+  for (void* p : allocs) cudaFree(p);
+}
+void* FFNet::alloc(size_t bytes) {
+  void* p = nullptr;
+  LPM_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+  allocs.push_back(p);
+  return p;
+}
+
+void tc_selftest(lpm_context& ctx, const float* A, const float* B, float* D, int N, int K, int amn,
+                 int bmn) {
+  if (N < 16 || N > 128 || N % 16 || K < 16 || K > 128 || K % 16)
+    throw Error(LPM_ERR_ARG, "tcgen05 self-test: N and K must be multiples of 16 in [16, 128]");
+  static bool attr = false;
+  if (!attr) {
+    LPM_CUDA(cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  2 * kSelfBuf));
+    attr = true;
+  }
+  k_tc_selftest<<<1, 128, 2 * kSelfBuf, ctx.stream>>>(A, B, D, N, K, amn, bmn, ctx.d_err);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+void ff_prepare_kernels() {
+  LPM_CUDA(cudaFuncSetAttribute(k_ff_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmInfer));
+  LPM_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrain));
+}
+
+void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int64_t wstride,
+                   double eps, double rho_min) {
+  LPM_CUDA(cudaMemsetAsync(d.counter, 0, sizeof(int), ctx.stream));
+  MlpArgs a;
+  a.xt = d.xt;
+  a.tperm = d.tperm;
+  a.ntgt = d.ntgt;
+  a.nblocks = d.nblocks;
+  a.cd = d.cd;
+  a.lrn = d.lrn;
+  a.cnt = d.cnt;
+  a.wbf = net.wbf;
+  a.norm = net.norm;
+  a.wout = wout;
+  a.wstride = wstride;
+  a.eps = float(eps);
+  a.rho_min = float(rho_min);
+  a.counter = d.counter;
+  a.err = ctx.d_err;
+  const int grid = int(std::min<int64_t>(d.nblocks, ctx.num_sms));
+  k_ff_mlp<<<grid, 128, kSmInfer, ctx.stream>>>(a);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
+}
+
+}  // namespace lpm
+
+// ---------------------------------------------------------------------------
+// lpm_farfield: network management and training
+// ---------------------------------------------------------------------------
+namespace {
+void ensure_net(lpm_farfield& ff) {
+  if (ff.net) return;
+  ff.net = new lpm::FFNet();
+  ff.net->wbf = static_cast<uint16_t*>(ff.net->alloc(sizeof(uint16_t) * lpm::kNParam));
+  ff.net->norm = static_cast<float*>(ff.net->alloc(sizeof(float) * 128));
+}
+}  // namespace
+
+void lpm_farfield::init_net(uint64_t seed) {
+  using namespace lpm;
+  w.assign(kNParam, 0.f);
+  std::mt19937_64 rng(seed);
+  auto fill = [&](int off, int rows, int cols, int fan, int nrows_live, int bias_col) {
+    const float k = 1.f / std::sqrt(float(fan));
+    std::uniform_real_distribution<float> u(-k, k);
+    for (int r = 0; r < rows; ++r)
+      for (int c = 0; c < cols; ++c) {
+        float v = u(rng);
+        if (r >= nrows_live || c == bias_col) v = 0.f;
+        w[off + r * cols + c] = v;
+      }
+  };
+  fill(0, kHid, kIn, kNFeat - 1, kBiasHid, kBiasIn);
+  fill(kW1, kHid, kHid, kHid - 1, kBiasHid, kBiasHid);
+  fill(kW1 + kW2, kHid, kHid, kHid - 1, kBiasHid, kBiasHid);
+  fill(kW1 + kW2 + kW3, kOut, kHid, kHid - 1, 3, kBiasHid);
+  // inputs beyond the bias feature are zero; identity normalisation
+  norm.assign(2 * kIn + 1, 0.f);
+  for (int i = 0; i < kIn; ++i) norm[kIn + i] = i <= kBiasIn ? 1.f : 0.f;
+  norm[2 * kIn] = 1.f;
+}
+
+void lpm_farfield::upload_net() {
+  using namespace lpm;
+  ensure_net(*this);
+  float* dw = nullptr;
+  LPM_CUDA(cudaMalloc(&dw, sizeof(float) * kNParam));
+  cudaError_t e = cudaMemcpyAsync(dw, w.data(), sizeof(float) * kNParam, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    k_mlp_image<<<(kNParam + 255) / 256, 256, 0, ctx->stream>>>(dw, net->wbf);
+    ctx->launches++;
+    e = cudaMemcpyAsync(net->norm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice,
+                        ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dw);
+  LPM_CUDA(e);
+}
+
+namespace {
+
+// Device buffers of one training run.
+struct TrainBufs {
+  std::vector<void*> p;
+  void* alloc(size_t n) {
+    void* q = nullptr;
+    LPM_CUDA(cudaMalloc(&q, std::max<size_t>(n, 256)));
+    p.push_back(q);
+    return q;
+  }
+  ~TrainBufs() {
+    for (void* q : p) cudaFree(q);
+  }
+};
+
+void set_train_attr() { lpm::ff_prepare_kernels(); }
+
+// Random vortex field: 1-4 Gaussian vortices (MULTI_GAUSSIAN parameters) or
+// a Rossby-Haurwitz 5-4 wave of random amplitude.
+void random_field(std::mt19937_64& rng, int& kind, std::vector<double>& prm) {
+  std::uniform_real_distribution<double> u(0.0, 1.0);
+  const double pi = 3.141592653589793;
+  if (u(rng) < 0.3) {
+    const double w = 2 * pi / 12.5 * (0.5 + u(rng));
+    kind = LPM_IC_RH54;
+    prm = {w, -w * (0.5 + u(rng))};
+    return;
+  }
+  kind = LPM_IC_MULTI_GAUSSIAN;
+  const int k = 1 + int(u(rng) * 4) % 4;
+  prm = {double(k)};
+  for (int i = 0; i < k; ++i) {
+    const double z = 2 * u(rng) - 1, lon = 2 * pi * u(rng), lat = std::asin(z);
+    const double amp = pi + 3 * pi * u(rng), wd = 0.1 + 0.3 * u(rng);
+    prm.insert(prm.end(), {amp, 1.0 / wd, lon, lat});
+  }
+}
+
+}  // namespace
+
+std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
+  using namespace lpm;
+  ensure_net(*this);
+  set_train_attr();
+  cudaStream_t st = ctx->stream;
+  const int64_t n = cfg.nsamples;
+  if (n < 128 || cfg.batch < 128 || cfg.batch % 128 || cfg.epochs < 1)
+    throw Error(LPM_ERR_ARG, "far field training: nsamples >= 128, batch a multiple of 128, epochs >= 1");
+  TrainBufs tb;
+  float* X = static_cast<float*>(tb.alloc(sizeof(float) * kIn * n));
+  float* Y = static_cast<float*>(tb.alloc(sizeof(float) * 4 * n));
+  // ---- samples from seeded random vortex fields --------------------------
+  std::mt19937_64 rng(cfg.seed);
+  int64_t rows = 0;
+  const double c0 = chord_c0(3, cfg.eps);
+  struct MeshCache {
+    std::vector<double> vx, fx, fa;
+    std::vector<uint8_t> fm;
+  };
+  std::vector<MeshCache> meshes(32);
+  int field = 0;
+  while (rows < n) {
+    const int L = cfg.level_min + int(rng() % uint64_t(cfg.level_max - cfg.level_min + 1));
+    MeshCache& mc = meshes[L];
+    if (mc.fx.empty()) {
+      int64_t nv, nf;
+      mesh_sizes(LPM_MESH_ICOS_TRI, L, &nv, &nf);
+      mc.vx.resize(3 * nv);
+      mc.fx.resize(3 * nf);
+      mc.fa.resize(nf);
+      mc.fm.resize(nf);
+      mesh_build(LPM_MESH_ICOS_TRI, L, 1.0, mc.vx.data(), mc.fx.data(), mc.fa.data(), mc.fm.data());
+    }
+    int kind;
+    std::vector<double> prm;
+    random_field(rng, kind, prm);
+    const int64_t nf = int64_t(mc.fa.size());
+    std::vector<double> z(nf);
+    ic_eval(kind, prm.data(), int(prm.size()), 3, nf, mc.fx.data(), z.data());
+    std::vector<double> sx;
+    std::vector<double> sg;
+    for (int64_t i = 0; i < nf; ++i)
+      if (!mc.fm[i]) {
+        sx.insert(sx.end(), {mc.fx[3 * i], mc.fx[3 * i + 1], mc.fx[3 * i + 2]});
+        sg.push_back(z[i] * mc.fa[i]);
+      }
+    const int64_t ns = int64_t(sg.size());
+    TreeTopo tp = build_tree(sx.data(), ns, nullptr, 0, leaf_max);
+    const int nc = int(tp.start.size());
+    std::vector<double4> sd(ns);
+    std::vector<float4> sf(ns);
+    for (int64_t k = 0; k < ns; ++k) {
+      const int j = tp.perm[k];
+      sd[k] = make_double4(sx[3 * j], sx[3 * j + 1], sx[3 * j + 2], sg[j]);
+      sf[k] = make_float4(float(sd[k].x), float(sd[k].y), float(sd[k].z), float(sd[k].w));
+    }
+    std::vector<int4> ci(nc);
+    std::vector<int> jobs;
+    for (int i = 0; i < nc; ++i) {
+      ci[i] = make_int4(tp.start[i], tp.count[i], tp.child0[i], tp.nchild[i]);
+      if (tp.count[i] >= 8)
+        for (int r = 0; r < 2; ++r) jobs.push_back(i);
+    }
+    std::shuffle(jobs.begin(), jobs.end(), rng);
+    // at most a quarter of the samples from one field
+    const int64_t cap = std::max<int64_t>(1, std::min<int64_t>((n - rows + 127) / 128, (n / 4 + 127) / 128));
+    if (int64_t(jobs.size()) > cap) jobs.resize(size_t(cap));
+    TrainBufs fb;
+    double4* dsd = static_cast<double4*>(fb.alloc(sizeof(double4) * ns));
+    float4* dsf = static_cast<float4*>(fb.alloc(sizeof(float4) * ns));
+    int4* dci = static_cast<int4*>(fb.alloc(sizeof(int4) * nc));
+    float* dcd = static_cast<float*>(fb.alloc(sizeof(float) * kCellF * size_t(nc)));
+    int* djobs = static_cast<int*>(fb.alloc(sizeof(int) * jobs.size()));
+    LPM_CUDA(cudaMemcpyAsync(dsd, sd.data(), sizeof(double4) * ns, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaMemcpyAsync(dsf, sf.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaMemcpyAsync(dci, ci.data(), sizeof(int4) * nc, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(int) * jobs.size(), cudaMemcpyHostToDevice, st));
+    ff_cells(*ctx, dsf, dci, nc, dcd);
+    k_ff_samples<<<int(jobs.size()), 128, 0, st>>>(dcd, dci, dsd, djobs, int(jobs.size()),
+                                                    cfg.seed * 7919 + uint64_t(field), float(theta),
+                                                    float(rho_min), float(cfg.eps), c0, X, Y, rows, n);
+    ctx->launches++;
+    LPM_CUDA(cudaGetLastError());
+    LPM_CUDA(cudaStreamSynchronize(st));
+    rows += int64_t(jobs.size()) * 128;
+    field++;
+  }
+  // ---- normalisation -----------------------------------------------------
+  const int sblk = 512;
+  double* spart = static_cast<double*>(tb.alloc(sizeof(double) * sblk * (2 * kIn + 1)));
+  k_ff_stats<<<sblk, 256, 0, st>>>(X, Y, n, spart);
+  std::vector<double> hs(size_t(sblk) * (2 * kIn + 1));
+  LPM_CUDA(cudaMemcpyAsync(hs.data(), spart, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, st));
+  LPM_CUDA(cudaStreamSynchronize(st));
+  std::vector<double> tot(2 * kIn + 1, 0.0);
+  for (int b = 0; b < sblk; ++b)
+    for (int f = 0; f <= 2 * kIn; ++f) tot[f] += hs[size_t(b) * (2 * kIn + 1) + f];
+  norm.assign(2 * kIn + 1, 0.f);
+  for (int f = 0; f < kIn; ++f) {
+    const double mu = tot[f] / double(n);
+    const double var = std::max(0.0, tot[kIn + f] / double(n) - mu * mu);
+    if (f == kBiasIn) {
+      norm[f] = 0.f;
+      norm[kIn + f] = 1.f;
+    } else if (f > kBiasIn || var <= 1e-30) {
+      norm[f] = float(mu);
+      norm[kIn + f] = 0.f;
+    } else {
+      norm[f] = float(mu);
+      norm[kIn + f] = float(1.0 / std::sqrt(var));
+    }
+  }
+  norm[2 * kIn] = float(std::sqrt(tot[2 * kIn] / (3.0 * double(n))));
+  float* dnorm = static_cast<float*>(tb.alloc(sizeof(float) * (2 * kIn + 1)));
+  LPM_CUDA(cudaMemcpyAsync(dnorm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice, st));
+  uint16_t* Xb = static_cast<uint16_t*>(tb.alloc(sizeof(uint16_t) * kIn * n));
+  float* Yn = static_cast<float*>(tb.alloc(sizeof(float) * 4 * n));
+  k_ff_normalise<<<unsigned((n + 255) / 256), 256, 0, st>>>(X, Y, n, dnorm, Xb, Yn);
+  ctx->launches += 2;
+  // ---- Adam ----------------------------------------------------------------
+  if (w.size() != size_t(kNParam)) init_net(cfg.seed);
+  {
+    std::vector<float> keep = norm;
+    upload_net();  // BF16 image of the initial weights
+    norm = keep;
+  }
+  float* wm = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));
+  float* mm = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));
+  float* vv = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));
+  LPM_CUDA(cudaMemcpyAsync(wm, w.data(), sizeof(float) * kNParam, cudaMemcpyHostToDevice, st));
+  LPM_CUDA(cudaMemsetAsync(mm, 0, sizeof(float) * kNParam, st));
+  LPM_CUDA(cudaMemsetAsync(vv, 0, sizeof(float) * kNParam, st));
+  const int tiles = cfg.batch / 128;
+  float* gpart = static_cast<float*>(tb.alloc(sizeof(float) * kNParam * size_t(tiles)));
+  float* lpart = static_cast<float*>(tb.alloc(sizeof(float) * size_t(tiles) * 1024));
+  const int64_t steps_per_epoch = std::max<int64_t>(1, n / cfg.batch);
+  const int64_t total = steps_per_epoch * cfg.epochs;
+  std::vector<float> hist;
+  const float b1 = 0.9f, b2 = 0.999f;
+  int64_t step = 0;
+  for (int ep = 0; ep < cfg.epochs; ++ep) {
+    // affine permutation of the sample order for this epoch
+    uint64_t pa = (rng() | 1ULL) % uint64_t(n);
+    while (std::gcd(pa, uint64_t(n)) != 1) pa = (pa + 2) % uint64_t(n);
+    const uint64_t pb = rng() % uint64_t(n);
+    double eloss = 0;
+    // loss per step, summed on the host at the end of the epoch
+    std::vector<float> lh(size_t(tiles) * std::min<int64_t>(steps_per_epoch, 1024));
+    for (int64_t s = 0; s < steps_per_epoch; ++s, ++step) {
+      TrainArgs a;
+      a.Xb = Xb;
+      a.Yn = Yn;
+      a.n = n;
+      a.pa = pa;
+      a.pb = pb;
+      a.row0 = s * cfg.batch;
+      a.inv_batch = 1.f / float(cfg.batch);
+      a.wbf = net->wbf;
+      a.gpart = gpart;
+      a.lpart = lpart + (s % 1024) * tiles;
+      a.err = ctx->d_err;
+      k_mlp_train<<<tiles, 128, kSmTrain, st>>>(a);
+      // cosine learning rate after a short warm-up
+      const double fr = double(step) / double(total);
+      const double warm = std::min(1.0, double(step + 1) / 100.0);
+      const float lr = float(cfg.lr * warm * 0.5 * (1.0 + std::cos(3.141592653589793 * fr)));
+      const float bc1 = 1.f - std::pow(b1, float(step + 1)), bc2 = 1.f - std::pow(b2, float(step + 1));
+      k_mlp_adam<<<(kNParam + 255) / 256, 256, 0, st>>>(gpart, tiles, wm, mm, vv, net->wbf, lr, b1,
+                                                         b2, bc1, bc2, 1e-8f);
+      ctx->launches += 2;
+      if ((s % 1024) == 1023 || s + 1 == steps_per_epoch) {
+        const int64_t ns = (s % 1024) + 1;
+        LPM_CUDA(cudaMemcpyAsync(lh.data(), lpart, sizeof(float) * tiles * ns, cudaMemcpyDeviceToHost, st));
+        LPM_CUDA(cudaStreamSynchronize(st));
+        for (int64_t k = 0; k < tiles * ns; ++k) eloss += lh[k];
+      }
+    }
+    LPM_CUDA(cudaGetLastError());
+    hist.push_back(float(eloss / (double(steps_per_epoch) * cfg.batch)));
+  }
+  LPM_CUDA(cudaMemcpyAsync(w.data(), wm, sizeof(float) * kNParam, cudaMemcpyDeviceToHost, st));
+  LPM_CUDA(cudaMemcpyAsync(net->norm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice, st));
+  LPM_CUDA(cudaStreamSynchronize(st));
+  check_device_error(*ctx);
+  trained = true;
+  return hist;
+}
+
+void lpm_farfield::grad(const float* x_host, const float* y_host, int n, float* g_host) {
+  using namespace lpm;
+  ensure_net(*this);
+  set_train_attr();
+  if (n < 128 || n % 128) throw Error(LPM_ERR_ARG, "grad check: n must be a positive multiple of 128");
+  if (w.size() != size_t(kNParam)) throw Error(LPM_ERR_STATE, "grad check: no weights");
+  cudaStream_t st = ctx->stream;
+  TrainBufs tb;
+  std::vector<uint16_t> xb(size_t(n) * kIn);
+  for (size_t i = 0; i < xb.size(); ++i) {
+    __nv_bfloat16 h = __float2bfloat16(x_host[i]);
+    xb[i] = *reinterpret_cast<uint16_t*>(&h);
+  }
+  std::vector<float> yn(size_t(n) * 4, 0.f);
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < 3; ++k) yn[size_t(r) * 4 + k] = y_host[size_t(r) * 3 + k];
+  uint16_t* dX = static_cast<uint16_t*>(tb.alloc(sizeof(uint16_t) * xb.size()));
+  float* dY = static_cast<float*>(tb.alloc(sizeof(float) * yn.size()));
+  const int tiles = n / 128;
+  float* gpart = static_cast<float*>(tb.alloc(sizeof(float) * kNParam * size_t(tiles)));
+  float* lpart = static_cast<float*>(tb.alloc(sizeof(float) * tiles));
+  LPM_CUDA(cudaMemcpyAsync(dX, xb.data(), sizeof(uint16_t) * xb.size(), cudaMemcpyHostToDevice, st));
+  LPM_CUDA(cudaMemcpyAsync(dY, yn.data(), sizeof(float) * yn.size(), cudaMemcpyHostToDevice, st));
+  upload_net();
+  TrainArgs a;
+  a.Xb = dX;
+  a.Yn = dY;
+  a.n = n;
+  a.pa = 1;
+  a.pb = 0;
+  a.row0 = 0;
+  a.inv_batch = 1.f / float(n);
+  a.wbf = net->wbf;
+  a.gpart = gpart;
+  a.lpart = lpart;
+  a.err = ctx->d_err;
+  k_mlp_train<<<tiles, 128, kSmTrain, st>>>(a);
+  ctx->launches++;
+  LPM_CUDA(cudaGetLastError());
+  std::vector<float> gp(size_t(kNParam) * tiles);
+  LPM_CUDA(cudaMemcpyAsync(gp.data(), gpart, sizeof(float) * gp.size(), cudaMemcpyDeviceToHost, st));
+  LPM_CUDA(cudaStreamSynchronize(st));
+  check_device_error(*ctx);
+  for (int i = 0; i < kNParam; ++i) {
+    double s = 0;
+    for (int p = 0; p < tiles; ++p) s += gp[size_t(p) * kNParam + i];
+    g_host[i] = float(s);
+  }
+}

@@ -115,6 +115,17 @@ struct EnsPk {
   }
 };
 
+// Positions of all targets (T x 3) and of the sources (nsrc x 3), FP64.
+__global__ void k_snapshot(Tg g, const int* src2slot, int64_t nsrc, double* tx, double* sx) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i < g.T) {
+    for (int c = 0; c < 3; ++c) tx[3 * i + c] = g.x(i, c);
+  } else if (i < g.T + nsrc) {
+    const int64_t s = i - g.T;
+    for (int c = 0; c < 3; ++c) sx[3 * s + c] = g.fx(src2slot[s], c);
+  }
+}
+
 // Pack target t (and its source record when it is an unmasked face) at
 // position p with vorticity z.
 template <class TG, class PK>

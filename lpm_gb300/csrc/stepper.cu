@@ -24,6 +24,7 @@
 
 #include "lpm_host.hpp"
 #include "nbody.cuh"
+#include "farfield.hpp"
 #include "stage.cuh"
 
 
@@ -49,6 +50,11 @@ struct lpm_stepper_base {
   void *tgt = nullptr, *src = nullptr;
   double* part = nullptr;
   double* sgbuf = nullptr;  // [0] = sum, [8..] partials
+
+  // optional octree far field in place of the direct sum (BVE, FP64 chord packs)
+  lpm_farfield* ff = nullptr;
+  int ff_every = 0;
+  int64_t ff_steps = 0;
 
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -144,11 +150,46 @@ struct lpm_stepper_base {
     k.tself = tself;
     k.src = src;
     k.part = part;
-    k.nchunks = plan.nchunks;
+    k.nchunks = ff ? 1 : plan.nchunks;
     k.tpad = plan.ntgt_pad;
     return k;
   }
+  // Builds the far field's tree from the current positions when it is due
+  // (first step, then every ff_every steps); outside any graph capture.
+  void ff_prepare(const lpm::Tg& g) {
+    if (!ff) return;
+    const bool due = !ff->built() || (ff_every > 0 && ff_steps % ff_every == 0);
+    ff_steps++;
+    if (!due) return;
+    lpm_context& c = *ctx;
+    c.arena.reset();
+    c.arena.reserve(sizeof(double) * 3 * size_t(T + nsrc) + 4096);
+    double* d = static_cast<double*>(c.arena.take(sizeof(double) * 3 * size_t(T + nsrc)));
+    const int64_t n = T + nsrc;
+    lpm::k_snapshot<<<unsigned((n + 255) / 256), 256, 0, c.stream>>>(g, src2slot, nsrc, d, d + 3 * T);
+    c.launches++;
+    std::vector<double> h(3 * size_t(n));
+    LPM_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c.stream));
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    ff->build(h.data() + 3 * T, nsrc, h.data(), T);
+  }
   void nbody() {
+    if (ff) {
+      cudaEvent_t e[2];
+      const bool timed = flags & LPM_STEP_TIME_NBODY;
+      if (timed) {
+        LPM_CUDA(cudaEventCreate(&e[0]));
+        LPM_CUDA(cudaEventCreate(&e[1]));
+        LPM_CUDA(cudaEventRecord(e[0], ctx->stream));
+      }
+      ff->evaluate(tgt, src, part, plan.ntgt_pad, c0(), eps);
+      if (timed) {
+        LPM_CUDA(cudaEventRecord(e[1], ctx->stream));
+        timers.push_back(e[0]);
+        timers.push_back(e[1]);
+      }
+      return;
+    }
     if (precision != LPM_FP64 && want_psi && ndim == 3)
       lpm::sum_strengths(*ctx, src, precision == LPM_FP32C, nsrc, sgbuf, sgbuf + 8);
     if (flags & LPM_STEP_TIME_NBODY) {
@@ -251,8 +292,11 @@ struct lpm_bve_rk4 : lpm_stepper_base {
     P.reproject = flags & LPM_STEP_REPROJECT;
     P.c0 = c0();
 
-    std::vector<char> kk(sizeof(lpm::Tg));
+    ff_prepare(g);
+    std::vector<char> kk(sizeof(lpm::Tg) + sizeof(void*));
     std::memcpy(kk.data(), &g, sizeof(g));
+    const void* fd = ff ? static_cast<const void*>(ff->d) : nullptr;
+    std::memcpy(kk.data() + sizeof(g), &fd, sizeof(fd));
     const int64_t nb = (T + 255) / 256;
     run(kk, [&]() {
       if (T == 0) return;
@@ -433,6 +477,19 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
   } catch (...) {
     return lpm::handle_exception();
   }
+}
+
+int lpm_bve_rk4_set_farfield(lpm_bve_rk4* st, lpm_farfield* ff, int rebuild_every) {
+  if (!st) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_set_farfield: null stepper");
+  if (ff && st->precision != LPM_FP64_CHORD)
+    return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_set_farfield: the stepper must use LPM_FP64_CHORD");
+  if (ff && ff->ctx != st->ctx)
+    return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_set_farfield: far field and stepper contexts differ");
+  if (rebuild_every < 0) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_set_farfield: rebuild_every < 0");
+  st->ff = ff;
+  st->ff_every = rebuild_every;
+  st->ff_steps = 0;
+  return LPM_OK;
 }
 
 int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches) {
