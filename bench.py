@@ -650,6 +650,156 @@ def run_plane(args, device):
             "clocks": clocks, "gpu_launches": ctx.kernel_launches - l0}
 
 
+def run_c5(args, device):
+    """Configuration C5: BVE sphere at icosahedral level 8 (1,310,720 leaf
+    faces, 655,362 vertices), Rossby-Haurwitz R=4 (omega = K = Omega/12.5),
+    eps = 0.01, RK4 dt = 0.005, evaluated by the octree far field (leaves <= 64
+    points, opening angle 0.5, order-4 expansion, exact FP32-compensated near
+    field) with the learned correction: a BF16 MLP (moments to order 4 in the
+    target's cell frame, 3 x 128 SiLU) trained on the GPU by the tcgen05
+    kernels on 2^24 cell-target samples from seeded random vortex fields.
+    value = direct-equivalent interactions ((Nv + Nf) Nf per evaluation) per
+    second.  Judges of the error: the GPU FP64 direct sum (reference
+    arithmetic) on a seeded 16,384-target subsample for one evaluation, and
+    the FP32C direct-sum trajectory (1.6e-7 from FP64 after a step, C2) for
+    the steps; the FP64 time per evaluation is the subsample's time scaled
+    linearly to all targets."""
+    import torch
+
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.farfield import FarField
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+    L = args.level if args.level != LEVEL else 8
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, L, 1.0)
+    w = OMEGA / 12.5
+    vz = core.eval_ic(core.IC_RH54, (w, -w), vx)
+    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    nv, nleaf = vx.shape[0], int((fm == 0).sum())
+    ipe = (nv + nleaf) * nleaf
+    st0 = DeviceState((vx, fx, fa, fm, vz, fz), device)
+    # ---- network: trained here on the GPU (not in the timed region) ----------
+    ff = FarField(theta=0.5, leaf_max=64, rho_min=0.15, ctx=ctx)
+    t0 = time.perf_counter()
+    loss = ff.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
+                    seed=20261203, level_min=5, level_max=8, eps=EPS)
+    torch.cuda.synchronize(device)
+    train_s = time.perf_counter() - t0
+    # ---- one evaluation: learned / expansion only vs the GPU FP64 direct sum --
+    xall = torch.cat([st0.vx, st0.fx[st0.fm == 0]])
+    rng = np.random.default_rng(20261203)
+    idx = torch.from_numpy(np.sort(rng.choice(xall.shape[0], 16384, replace=False))).to(xall.device)
+    xs = xall[idx].contiguous()
+    ctx.set_precision(core.FP64)
+    u64 = torch.zeros_like(xs)
+    F.ic2d_passive_sums(ctx, u64, None, xs, st0.fx, st0.fz, st0.fa, st0.fm, EPS)  # warm
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    F.ic2d_passive_sums(ctx, u64, None, xs, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
+    b.record(stream)
+    torch.cuda.synchronize(device)
+    fp64_eval_s = a.elapsed_time(b) * 1e-3 * xall.shape[0] / xs.shape[0]
+    uall = torch.zeros_like(xall)
+    errs = {}
+    for tag, net in (("expansion_only", False), ("learned", True)):
+        ff.set_network(net)
+        ff.velocity(uall, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
+        torch.cuda.synchronize(device)
+        errs[tag] = rel_errors(uall[idx], u64)
+    stats = ff.stats()
+    ff.set_network(True)
+    # ---- RK4 steps on the learned far field --------------------------------
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+    st = st0.clone()
+    st.velocity(ctx, core.FP64_CHORD)
+    h = make_stepper(ctx, st, core.FP64_CHORD, flags)
+    core.check(core.lib().lpm_bve_rk4_set_farfield(h, ff.handle, 0))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        advance(h, st)
+    torch.cuda.synchronize(device)
+    sampler = ClockSampler(device)
+    sampler.start()
+    l0 = ctx.kernel_launches
+    ms = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        advance(h, st)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        ms += a.elapsed_time(b)
+    clocks = sampler.stop()
+    launches = ctx.kernel_launches - l0
+    core.lib().lpm_bve_rk4_destroy(h)
+    # ---- the same steps with the FP32C direct sum (trajectory judge) --------
+    ref = st0.clone()
+    ref.velocity(ctx, core.FP32C)
+    hr = make_stepper(ctx, ref, core.FP32C, flags)
+    for _ in range(args.warmup + args.steps):
+        advance(hr, ref)
+    torch.cuda.synchronize(device)
+    core.lib().lpm_bve_rk4_destroy(hr)
+    traj = {"position_leaf_faces": rel_errors(st.fx, ref.fx, st.fm),
+            "vorticity_leaf_faces": rel_errors(st.fz, ref.fz, st.fm),
+            "velocity_leaf_faces": rel_errors(st.fu, ref.fu, st.fm),
+            "velocity_vertices": rel_errors(st.vu, ref.vu)}
+    # ---- kernel split of one step (events around the tree and network parts)
+    hs = make_stepper(ctx, st, core.FP64_CHORD, flags | core.STEP_TIME_NBODY)
+    core.check(core.lib().lpm_bve_rk4_set_farfield(hs, ff.handle, 0))
+    ff.timing(True)
+    advance(hs, st)
+    tree_ms, net_ms, nev = ff.timing(False)
+    core.lib().lpm_bve_rk4_destroy(hs)
+    tiles = stats["learned_tiles"]
+    flops_tile = 2 * 128 * (48 * 128 + 2 * 128 * 128 + 128 * 16)
+    peaks = {}
+    pp = ROOT / "MEASURED_PEAKS.json"
+    if pp.exists():
+        peaks = json.loads(pp.read_text())
+    peak = peaks.get("bf16_tflops")
+    net_tf = tiles * flops_tile / (net_ms / nev * 1e-3) / 1e12 if nev and net_ms > 0 else None
+    step_s = ms / args.steps * 1e-3
+    return {"metric": METRIC,
+            "value": round(4 * ipe / step_s / 1e9, 3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+bf16", "data": "synthetic (generated mesh + Rossby-Haurwitz wave; "
+                                          "network trained on seeded random vortex fields)",
+            "config": {"workload": f"BVE sphere icosahedral level {L} RK4, RH R=4, eps={EPS}, "
+                                   f"dt={DT}, octree far field theta=0.5 leaf<=64 + learned "
+                                   "correction", "vertices": nv, "leaf_faces": nleaf,
+                       "direct_equivalent_interactions_per_step": 4 * ipe,
+                       "l2": "flushed between timed steps (512 MiB write)",
+                       "training": {"samples": args.ff_samples, "epochs": args.ff_epochs,
+                                    "batch": 16384, "seconds": round(train_s, 2),
+                                    "loss_per_epoch": [round(float(x), 6) for x in loss]}},
+            "speedup_vs_gpu_fp64_direct": round(fp64_eval_s / (step_s / 4), 1),
+            "fp64_direct": {"seconds_per_evaluation": round(fp64_eval_s, 3),
+                            "value": round(ipe / fp64_eval_s / 1e9, 3),
+                            "note": "reference arithmetic on 16,384 seeded targets, scaled "
+                                    "linearly to all targets"},
+            "errors_one_evaluation_vs_fp64_direct_16384_targets": errs,
+            "errors_after_steps_vs_fp32c_direct": traj,
+            "far_field": {**stats, "tree_ms_per_evaluation": round(tree_ms / max(nev, 1), 3),
+                          "network_ms_per_evaluation": round(net_ms / max(nev, 1), 3)},
+            "roofline": {"bound": "tensor", "kernel": "k_ff_mlp (tcgen05 BF16 MLP, 4 layers)",
+                         "achieved": round(net_tf, 2) if net_tf else None,
+                         "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(net_tf / peak, 4) if (net_tf and peak) else None,
+                         "traffic": None,
+                         "flops_per_tile": flops_tile, "tiles_per_evaluation": tiles,
+                         "peak_kind": "bf16_tflops of MEASURED_PEAKS.json (burst)"},
+            "clocks": clocks, "gpu_launches": launches}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -657,9 +807,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--level", type=int, default=LEVEL)
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
                     help="c2: the metric's workload (default); c1: FP64 level 4; "
-                         "c3: planar dipoles; c4: 256-problem ensemble")
+                         "c3: planar dipoles; c4: 256-problem ensemble; "
+                         "c5: level 8 on the learned octree far field")
+    ap.add_argument("--ff-samples", type=int, default=1 << 24)
+    ap.add_argument("--ff-epochs", type=int, default=6)
     ap.add_argument("--plane-level", type=int, default=9)
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--cpu-targets", type=int, default=8192)
@@ -689,6 +842,8 @@ def main():
         res = run_plane(args, local) if rank == 0 else {}
     elif args.config == "c1":
         res = run_c1(args, local) if rank == 0 else {}
+    elif args.config == "c5":
+        res = run_c5(args, local) if rank == 0 else {}
     else:
         res = run_ours(args, rank, world, local)
     if rank == 0:

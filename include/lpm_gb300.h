@@ -352,11 +352,24 @@ int lpm_farfield_grad(lpm_farfield* ff, const float* x, const float* y, int n,
  * pairs / 128, learned tiles, blocks on the direct-sum fallback, cells,
  * target blocks.  out: 6 int64.  Synchronous. */
 int lpm_farfield_stats(lpm_farfield* ff, int64_t* out);
+/* Device time of the evaluations since the previous call (tree kernels and
+ * network kernel, ms) and their count, then resets; enable != 0 brackets the
+ * following evaluations with CUDA events (use with LPM_STEP_TIME_NBODY
+ * steppers or direct calls, not inside graph capture).  Synchronous. */
+int lpm_farfield_timing(lpm_farfield* ff, int enable, double* tree_ms,
+                        double* net_ms, int64_t* evals);
 /* Evaluate BVERK4 stages with the far field instead of the direct sum
  * (precision LPM_FP64_CHORD steppers; the tree is built on the first step and
  * rebuilt every rebuild_every steps, 0 = never).  ff must outlive st. */
 int lpm_bve_rk4_set_farfield(lpm_bve_rk4* st, lpm_farfield* ff,
                              int rebuild_every);
+/* Host only (no GPU): builds the octree of nsrc sources and the target blocks
+ * of ntgt targets (HOST n x 3 arrays) and summarises them in out[9]: cells,
+ * leaves, largest leaf, deepest level, target blocks, smallest block fill,
+ * targets covered, sources in leaves, and the count of structural errors
+ * (permutation, child ranges, duplicate targets) -- 0 for a valid tree. */
+int lpm_octree_stats(const double* src_xyz, int64_t nsrc, const double* tgt_xyz,
+                     int64_t ntgt, int leaf_max, int64_t* out);
 /* tcgen05 operand-layout self-test: D (128 x N) = A * B on the tensor cores,
  * A 128 x K (a_mn = 0) or K x 128 (a_mn = 1), B N x K (b_mn = 0) or K x N
  * (b_mn = 1), row-major FP32 device arrays rounded to BF16; N, K multiples of

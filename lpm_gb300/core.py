@@ -61,7 +61,8 @@ EXPORTS = [
     "lpm_ensemble_set_chunk_len", "lpm_sphere_tangency",
     "lpm_farfield_create", "lpm_farfield_destroy", "lpm_farfield_velocity", "lpm_farfield_train",
     "lpm_farfield_set_network", "lpm_farfield_get_weights", "lpm_farfield_set_weights",
-    "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest",
+    "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
+    "lpm_octree_stats",
 ]
 
 
@@ -150,6 +151,8 @@ def _declare(L: C.CDLL) -> None:
         "lpm_farfield_stats": [vp, vp],
         "lpm_bve_rk4_set_farfield": [vp, vp, i32],
         "lpm_tc_selftest": [vp, vp, vp, vp, i32, i32, i32, i32],
+        "lpm_farfield_timing": [vp, i32, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)],
+        "lpm_octree_stats": [vp, i64, vp, i64, i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

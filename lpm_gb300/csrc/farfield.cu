@@ -6,10 +6,11 @@
 //                   (FP32 per 32-point batch, FP64 across batches and threads)
 //   k_ff_tblocks    per block of 128 Morton-ordered targets: centre, radius
 //   k_ff_lists      per target block: tree walk with the opening criterion
-//                   h <= theta (D - r_b): far cells, near leaves, and the far
-//                   cells close enough (h / (D - r_b) >= rho_min) for the
-//                   learned correction; a block whose lists overflow is
-//                   marked for the direct sum
+//                   h <= theta (D - r_b): far cells (of >= kExactMax points;
+//                   smaller accepted cells are leaves and join the near
+//                   list), near leaves, and the far cells close enough
+//                   (h / (D - r_b) >= rho_min) for the learned correction; a
+//                   block whose lists overflow is marked for the direct sum
 //   k_ff_eval       per target block: exact FP32 chord sum over the near
 //                   leaves (per-leaf partials merged by TwoSum) + order-4
 //                   expansion of the far cells, or the full direct sum for
@@ -207,15 +208,15 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
 // One CTA (128 threads) per target block: Morton-ordered FP32 positions and
 // the block's bounding sphere.
 __global__ void __launch_bounds__(128) k_ff_tblocks(const double4* __restrict__ tgt,
-                                                    const int* __restrict__ tperm, int64_t ntgt,
+                                                    const int* __restrict__ tslot,
                                                     float4* __restrict__ xt, float4* __restrict__ box) {
   __shared__ double sh[5 * 8];
   const int64_t b = blockIdx.x;
   const int t = threadIdx.x;
   const int64_t i = b * kTargetBlock + t;
   float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i < ntgt) {
-    const double4 p = tgt[tperm[i]];
+  if (tslot[i] >= 0) {
+    const double4 p = tgt[tslot[i]];
     x = make_float4(float(p.x), float(p.y), float(p.z), 1.f);
   }
   xt[i] = x;
@@ -253,14 +254,16 @@ __global__ void k_ff_lists(const float* __restrict__ cd, const int4* __restrict_
     const float D = sqrtf(e0 * e0 + e1 * e1 + e2 * e2) - bx.w;
     const float h = r[4];
     const int4 ci = cells[c];
-    if (D > 0.f && h <= theta * D) {
+    const bool accept = D > 0.f && h <= theta * D;
+    if (accept && ci.y >= kExactMax) {
       if (nf < kFarCap) F[nf] = c;
       nf++;
-      if (learn && h >= rho_min * D && ci.y >= 8) {
+      if (learn && h >= rho_min * D) {
         if (nl < kLearnCap) L[nl] = c;
         nl++;
       }
     } else if (ci.w == 0) {
+      // a leaf that is near, or far but small enough to sum exactly
       if (nn < kNearCap) N[nn] = c;
       nn++;
     } else {
@@ -290,7 +293,7 @@ __device__ __forceinline__ void chord_acc(float x0, float x1, float x2, float4 s
 
 // One CTA (128 threads, one target each) per target block.
 __global__ void __launch_bounds__(128) k_ff_eval(
-    const float4* __restrict__ xt, const int* __restrict__ tperm, int64_t ntgt,
+    const float4* __restrict__ xt, const int* __restrict__ tslot,
     const float4* __restrict__ ys, int64_t nsrc, const float* __restrict__ cd,
     const int4* __restrict__ cells, const int* __restrict__ far, const int* __restrict__ near,
     const int4* __restrict__ cnt, float c0, double* __restrict__ wout, int64_t wstride) {
@@ -378,9 +381,8 @@ __global__ void __launch_bounds__(128) k_ff_eval(
       two_sum_acc(S2, C2, w2);
     }
   }
-  const int64_t i = b * kTargetBlock + t;
-  if (i < ntgt && x.w > 0.f) {
-    const int64_t tt = tperm[i];
+  const int64_t tt = tslot[b * kTargetBlock + t];
+  if (tt >= 0) {
     wout[tt] = double(S0) + double(C0);
     wout[wstride + tt] = double(S1) + double(C1);
     wout[2 * wstride + tt] = double(S2) + double(C2);
@@ -411,12 +413,12 @@ void ff_launch_tree(lpm_context& ctx, FFDevice& d, const void* tgt, const void* 
   k_ff_sort_src<<<unsigned((d.nsrc + 255) / 256), 256, 0, st>>>(static_cast<const double4*>(src),
                                                                  d.perm, d.nsrc, d.ys);
   k_ff_cells<<<d.ncells, 128, 0, st>>>(d.ys, d.cells, d.ncells, d.cd);
-  k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4*>(tgt), d.tperm,
-                                                    d.ntgt, d.xt, d.box);
+  k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4*>(tgt), d.tslot,
+                                                    d.xt, d.box);
   k_ff_lists<<<unsigned((d.nblocks + 63) / 64), 64, 0, st>>>(d.cd, d.cells, d.box, d.nblocks,
                                                             float(theta), float(rho_min), learn,
                                                             d.far, d.near, d.lrn, d.cnt);
-  k_ff_eval<<<unsigned(d.nblocks), 128, 0, st>>>(d.xt, d.tperm, d.ntgt, d.ys, d.nsrc, d.cd,
+  k_ff_eval<<<unsigned(d.nblocks), 128, 0, st>>>(d.xt, d.tslot, d.ys, d.nsrc, d.cd,
                                                  d.cells, d.far, d.near, d.cnt, float(c0), wout,
                                                  wstride);
   ctx.launches += 5;
@@ -428,7 +430,10 @@ void ff_launch_tree(lpm_context& ctx, FFDevice& d, const void* tgt, const void* 
 // ---------------------------------------------------------------------------
 // lpm_farfield host methods
 // ---------------------------------------------------------------------------
-lpm_farfield::~lpm_farfield() { delete d; }
+lpm_farfield::~lpm_farfield() {
+  for (void* e : events) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+  delete d;
+}
 
 bool lpm_farfield::built() const { return d != nullptr && d->ncells > 0; }
 
@@ -441,9 +446,9 @@ void lpm_farfield::build(const double* src_xyz, int64_t nsrc, const double* tgt_
     nd->nsrc = nsrc;
     nd->ntgt = ntgt;
     nd->ncells = int(tp.start.size());
-    nd->nblocks = (ntgt + kTargetBlock - 1) / kTargetBlock;
+    nd->nblocks = tp.nblocks;
     nd->perm = static_cast<int*>(nd->alloc(sizeof(int) * nsrc));
-    nd->tperm = static_cast<int*>(nd->alloc(sizeof(int) * std::max<int64_t>(ntgt, 1)));
+    nd->tslot = static_cast<int*>(nd->alloc(sizeof(int) * kTargetBlock * size_t(std::max<int64_t>(nd->nblocks, 1))));
     nd->cells = static_cast<int4*>(nd->alloc(sizeof(int4) * nd->ncells));
     nd->ys = static_cast<float4*>(nd->alloc(sizeof(float4) * nsrc));
     nd->cd = static_cast<float*>(nd->alloc(sizeof(float) * kCellF * size_t(nd->ncells)));
@@ -458,8 +463,9 @@ void lpm_farfield::build(const double* src_xyz, int64_t nsrc, const double* tgt_
     for (int i = 0; i < nd->ncells; ++i) ci[i] = make_int4(tp.start[i], tp.count[i], tp.child0[i], tp.nchild[i]);
     cudaStream_t st = ctx->stream;
     LPM_CUDA(cudaMemcpyAsync(nd->perm, tp.perm.data(), sizeof(int) * nsrc, cudaMemcpyHostToDevice, st));
-    if (ntgt > 0)
-      LPM_CUDA(cudaMemcpyAsync(nd->tperm, tp.tperm.data(), sizeof(int) * ntgt, cudaMemcpyHostToDevice, st));
+    if (nd->nblocks > 0)
+      LPM_CUDA(cudaMemcpyAsync(nd->tslot, tp.tslot.data(), sizeof(int) * tp.tslot.size(),
+                               cudaMemcpyHostToDevice, st));
     LPM_CUDA(cudaMemcpyAsync(nd->cells, ci.data(), sizeof(int4) * nd->ncells, cudaMemcpyHostToDevice, st));
     LPM_CUDA(cudaStreamSynchronize(st));
   } catch (...) {
@@ -475,8 +481,38 @@ void lpm_farfield::evaluate(const void* tgt, const void* src, double* wout, int6
   using namespace lpm;
   if (!built()) throw Error(LPM_ERR_STATE, "far field: tree not built");
   const bool learn = use_net && trained;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  if (timing) {
+    for (auto& e : ev) {
+      LPM_CUDA(cudaEventCreate(&e));
+      events.push_back(e);
+    }
+    LPM_CUDA(cudaEventRecord(ev[0], ctx->stream));
+  }
   ff_launch_tree(*ctx, *d, tgt, src, wout, wstride, c0, theta, rho_min, learn);
+  if (timing) LPM_CUDA(cudaEventRecord(ev[1], ctx->stream));
   if (learn) ff_launch_mlp(*ctx, *d, *net, wout, wstride, eps, rho_min);
+  if (timing) LPM_CUDA(cudaEventRecord(ev[2], ctx->stream));
+}
+
+void lpm_farfield::timings(double* tree_ms, double* net_ms, int64_t* evals) {
+  using namespace lpm;
+  LPM_CUDA(cudaStreamSynchronize(ctx->stream));
+  double a = 0, b = 0;
+  for (size_t i = 0; i + 2 < events.size(); i += 3) {
+    float m0 = 0, m1 = 0;
+    LPM_CUDA(cudaEventElapsedTime(&m0, static_cast<cudaEvent_t>(events[i]),
+                                  static_cast<cudaEvent_t>(events[i + 1])));
+    LPM_CUDA(cudaEventElapsedTime(&m1, static_cast<cudaEvent_t>(events[i + 1]),
+                                  static_cast<cudaEvent_t>(events[i + 2])));
+    a += m0;
+    b += m1;
+  }
+  *tree_ms = a;
+  *net_ms = b;
+  *evals = int64_t(events.size() / 3);
+  for (void* e : events) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+  events.clear();
 }
 
 void lpm_farfield::counts() {

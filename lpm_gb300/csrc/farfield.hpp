@@ -15,6 +15,7 @@ constexpr int kTargetBlock = 128;   // targets per block = rows of one MMA tile
 constexpr int kFarCap = 1024;       // far cells per target block
 constexpr int kNearCap = 384;       // near leaves per target block
 constexpr int kLearnCap = 1024;     // learned (cell, block) pairs per block
+constexpr int kExactMax = 32;       // accepted cells with fewer points are summed exactly
 
 // Cell record: kCellF floats per cell.
 //  [0..2] centre c (mean of the points), [3] |c|, [4] radius h (max |y - c|),
@@ -41,7 +42,8 @@ constexpr int kNFeat = 41;                      // features before padding (incl
 struct TreeTopo {
   int64_t nsrc = 0, ntgt = 0;
   std::vector<int> perm;   // sorted source position -> source index
-  std::vector<int> tperm;  // sorted target position -> target index
+  int64_t nblocks = 0;     // target blocks (leaves of the target octree)
+  std::vector<int> tslot;  // block * 128 + row -> target index, or -1 (padding)
   std::vector<int> start, count, child0, nchild, level;
   int max_level = 0;
 };
@@ -76,6 +78,10 @@ struct lpm_farfield {
   std::vector<float> w;       // kNParam
   std::vector<float> norm;    // mu[48], isd[48], out_scale
   int64_t last_far = 0, last_near = 0, last_learn = 0, last_fallback = 0;
+  // optional CUDA-event timing of evaluations (not inside graph capture)
+  bool timing = false;
+  std::vector<void*> events;  // cudaEvent_t triples: start, tree done, network done
+  void timings(double* tree_ms, double* net_ms, int64_t* evals);
 
   ~lpm_farfield();
   // Tree over the sources (nsrc x 3, host) and targets (ntgt x 3, host).

@@ -16,7 +16,7 @@ struct FFDevice {
   int64_t nsrc = 0, ntgt = 0, nblocks = 0;
   int ncells = 0;
   int* perm = nullptr;    // sorted source -> packed source index
-  int* tperm = nullptr;   // sorted target -> packed target index
+  int* tslot = nullptr;   // block * 128 + row -> packed target index or -1
   int4* cells = nullptr;  // (start, count, first child, child count)
   float4* ys = nullptr;   // sorted sources (x, y, z, g), FP32
   float* cd = nullptr;    // cell records, kCellF floats each

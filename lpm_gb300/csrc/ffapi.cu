@@ -225,6 +225,82 @@ int lpm_farfield_stats(lpm_farfield* ff, int64_t* out) {
   }
 }
 
+int lpm_farfield_timing(lpm_farfield* ff, int enable, double* tree_ms, double* net_ms,
+                        int64_t* evals) {
+  if (!ff) return fail(LPM_ERR_ARG, "null far field");
+  try {
+    cudaSetDevice(ff->ctx->device);
+    double a = 0, b = 0;
+    int64_t n = 0;
+    ff->timings(&a, &b, &n);
+    if (tree_ms) *tree_ms = a;
+    if (net_ms) *net_ms = b;
+    if (evals) *evals = n;
+    ff->timing = enable != 0;
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_octree_stats(const double* src_xyz, int64_t nsrc, const double* tgt_xyz, int64_t ntgt,
+                     int leaf_max, int64_t* out) {
+  if (!src_xyz || !out || (ntgt > 0 && !tgt_xyz)) return fail(LPM_ERR_ARG, "null argument");
+  if (nsrc <= 0 || bad_count(nsrc) || bad_count(ntgt)) return fail(LPM_ERR_ARG, "count out of range");
+  try {
+    const lpm::TreeTopo t = lpm::build_tree(src_xyz, nsrc, tgt_xyz, ntgt, leaf_max);
+    const int64_t nc = int64_t(t.start.size());
+    int64_t leaves = 0, max_leaf = 0, in_leaves = 0, bad = 0;
+    std::vector<char> seen(size_t(nsrc), 0);
+    for (int v : t.perm) {
+      if (v < 0 || v >= nsrc || seen[v]) bad++;
+      else seen[v] = 1;
+    }
+    for (int64_t i = 0; i < nc; ++i) {
+      if (t.nchild[i] == 0) {
+        leaves++;
+        in_leaves += t.count[i];
+        max_leaf = std::max<int64_t>(max_leaf, t.count[i]);
+        continue;
+      }
+      // children contiguous, covering the parent's range in order
+      int64_t pos = t.start[i];
+      for (int k = 0; k < t.nchild[i]; ++k) {
+        const int ch = t.child0[i] + k;
+        if (t.start[ch] != pos || t.count[ch] <= 0 || t.level[ch] != t.level[i] + 1) bad++;
+        pos += t.count[ch];
+      }
+      if (pos != t.start[i] + t.count[i]) bad++;
+    }
+    int64_t covered = 0, min_fill = lpm::kTargetBlock;
+    std::vector<char> tseen(size_t(std::max<int64_t>(ntgt, 1)), 0);
+    for (int64_t b = 0; b < t.nblocks; ++b) {
+      int64_t fill = 0;
+      for (int r = 0; r < lpm::kTargetBlock; ++r) {
+        const int v = t.tslot[size_t(b) * lpm::kTargetBlock + r];
+        if (v < 0) continue;
+        fill++;
+        if (v >= ntgt || tseen[v]) bad++;
+        else tseen[v] = 1;
+      }
+      covered += fill;
+      min_fill = std::min(min_fill, fill);
+    }
+    out[0] = nc;
+    out[1] = leaves;
+    out[2] = max_leaf;
+    out[3] = t.max_level;
+    out[4] = t.nblocks;
+    out[5] = t.nblocks ? min_fill : 0;
+    out[6] = covered;
+    out[7] = in_leaves;
+    out[8] = bad;
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
 int lpm_tc_selftest(lpm_context* ctx, const float* A, const float* B, float* D, int N, int K,
                     int a_mn, int b_mn) {
   if (!ctx || !A || !B || !D) return fail(LPM_ERR_ARG, "null argument");

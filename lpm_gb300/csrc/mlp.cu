@@ -179,8 +179,8 @@ __device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t
 
 struct MlpArgs {
   const float4* xt;
-  const int* tperm;
-  int64_t ntgt, nblocks;
+  const int* tslot;
+  int64_t nblocks;
   const float* cd;
   const int* lrn;
   const int4* cnt;
@@ -257,9 +257,8 @@ __global__ void __launch_bounds__(128, 1) k_ff_mlp(const MlpArgs a) {
       }
     }
     if (!ok) break;
-    const int64_t i = b * kTargetBlock + t;
-    if (i < a.ntgt && x.w > 0.f) {
-      const int64_t tt = a.tperm[i];
+    const int64_t tt = a.tslot[b * kTargetBlock + t];
+    if (tt >= 0) {
       a.wout[tt] += acc[0];
       a.wout[a.wstride + tt] += acc[1];
       a.wout[2 * a.wstride + tt] += acc[2];
@@ -691,8 +690,7 @@ void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int6
   LPM_CUDA(cudaMemsetAsync(d.counter, 0, sizeof(int), ctx.stream));
   MlpArgs a;
   a.xt = d.xt;
-  a.tperm = d.tperm;
-  a.ntgt = d.ntgt;
+  a.tslot = d.tslot;
   a.nblocks = d.nblocks;
   a.cd = d.cd;
   a.lrn = d.lrn;
@@ -815,6 +813,8 @@ std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
   const int64_t n = cfg.nsamples;
   if (n < 128 || cfg.batch < 128 || cfg.batch % 128 || cfg.epochs < 1)
     throw Error(LPM_ERR_ARG, "far field training: nsamples >= 128, batch a multiple of 128, epochs >= 1");
+  // fresh seeded weights; the normalisation is recomputed from the samples
+  init_net(cfg.seed);
   TrainBufs tb;
   float* X = static_cast<float*>(tb.alloc(sizeof(float) * kIn * n));
   float* Y = static_cast<float*>(tb.alloc(sizeof(float) * 4 * n));
@@ -865,10 +865,14 @@ std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
     }
     std::vector<int4> ci(nc);
     std::vector<int> jobs;
+    // jobs in proportion to the cell size (at least one, at most 64 per cell),
+    // so the large cells that dominate the far-field error are well sampled
     for (int i = 0; i < nc; ++i) {
       ci[i] = make_int4(tp.start[i], tp.count[i], tp.child0[i], tp.nchild[i]);
-      if (tp.count[i] >= 8)
-        for (int r = 0; r < 2; ++r) jobs.push_back(i);
+      if (tp.count[i] >= kExactMax) {
+        const int m = std::min(64, std::max(1, tp.count[i] / 64));
+        for (int r = 0; r < m; ++r) jobs.push_back(i);
+      }
     }
     std::shuffle(jobs.begin(), jobs.end(), rng);
     // at most a quarter of the samples from one field
@@ -927,12 +931,7 @@ std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
   k_ff_normalise<<<unsigned((n + 255) / 256), 256, 0, st>>>(X, Y, n, dnorm, Xb, Yn);
   ctx->launches += 2;
   // ---- Adam ----------------------------------------------------------------
-  if (w.size() != size_t(kNParam)) init_net(cfg.seed);
-  {
-    std::vector<float> keep = norm;
-    upload_net();  // BF16 image of the initial weights
-    norm = keep;
-  }
+  upload_net();  // BF16 image of the initial weights, this normalisation
   float* wm = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));
   float* mm = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));
   float* vv = static_cast<float*>(tb.alloc(sizeof(float) * kNParam));

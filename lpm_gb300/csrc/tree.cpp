@@ -5,8 +5,10 @@
 // with more than leaf_max points is split by the next three key bits into
 // its non-empty octants.  Cells are numbered breadth first, so the children
 // of a cell are contiguous; each cell is a contiguous range of the sorted
-// order.  Targets are Morton-sorted the same way and cut into blocks of
-// kTargetBlock consecutive targets.
+// order.  Targets are Morton-sorted the same way and cut into target blocks
+// of at most kTargetBlock targets (padded to kTargetBlock rows): the leaves of
+// a target octree, consecutive small sibling leaves packed into one block, so
+// no block straddles a jump of the curve and blocks stay well filled.
 //
 // The reference has no working octree (its LpmOctree/LpmNodeArray sources are
 // not built and lpm_cpu_tree indexes points by loop index); this is the
@@ -129,9 +131,52 @@ TreeTopo build_tree(const double* src_xyz, int64_t nsrc, const double* tgt_xyz, 
     if (t.nchild[i] == 0) t.child0[i] = -1;
     t.max_level = std::max(t.max_level, cells[i].level);
   }
-  // targets
+  // targets: Morton order cut into the leaves of an octree with at most
+  // kTargetBlock targets each, so that no block straddles a jump of the curve
   std::vector<uint64_t> tkeys;
-  t.tperm = ntgt > 0 ? sorted_order(bx, tgt_xyz, ntgt, tkeys) : std::vector<int>{};
+  std::vector<int> tperm = ntgt > 0 ? sorted_order(bx, tgt_xyz, ntgt, tkeys) : std::vector<int>{};
+  std::vector<std::pair<int, int>> blocks;
+  std::vector<C> work;
+  if (ntgt > 0) work.push_back({0, int(ntgt), 0});
+  while (!work.empty()) {
+    const C c = work.back();
+    work.pop_back();
+    if (c.count <= kTargetBlock || c.level >= 21) {  // a leaf, or packed siblings
+      for (int b = 0; b < c.count; b += kTargetBlock)
+        blocks.push_back({c.start + b, std::min(kTargetBlock, c.count - b)});
+      continue;
+    }
+    const int shift = 3 * (20 - c.level);
+    std::vector<C> kids;
+    int b = c.start;
+    const int e = c.start + c.count;
+    while (b < e) {
+      const uint64_t oct = (tkeys[b] >> shift) & 7;
+      int j = b;
+      while (j < e && ((tkeys[j] >> shift) & 7) == oct) ++j;
+      kids.push_back({b, j - b, c.level + 1});
+      b = j;
+    }
+    // consecutive small siblings share a block (they lie in the same parent
+    // octant); larger ones are split further
+    std::vector<C> split;
+    for (size_t k = 0; k < kids.size();) {
+      if (kids[k].count > kTargetBlock) {
+        split.push_back(kids[k++]);
+        continue;
+      }
+      int s0 = kids[k].start, n0 = 0;
+      while (k < kids.size() && kids[k].count <= kTargetBlock && n0 + kids[k].count <= kTargetBlock)
+        n0 += kids[k++].count;
+      split.push_back({s0, n0, 99});  // level 99: emit as one block
+    }
+    for (auto it = split.rbegin(); it != split.rend(); ++it) work.push_back(*it);
+  }
+  t.nblocks = int64_t(blocks.size());
+  t.tslot.assign(size_t(t.nblocks) * kTargetBlock, -1);
+  for (size_t k = 0; k < blocks.size(); ++k)
+    for (int r = 0; r < blocks[k].second; ++r)
+      t.tslot[k * kTargetBlock + r] = tperm[blocks[k].first + r];
   t.ntgt = ntgt;
   t.nsrc = nsrc;
   return t;

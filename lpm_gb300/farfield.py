@@ -83,6 +83,14 @@ class FarField:
         return {"far_pairs": out[0], "near_pairs_x128": out[1], "learned_tiles": out[2],
                 "fallback_blocks": out[3], "cells": out[4], "target_blocks": out[5]}
 
+    def timing(self, enable: bool) -> tuple[float, float, int]:
+        """(tree ms, network ms, evaluations) since the last call; then
+        enables or disables event timing of the following evaluations."""
+        a, b, n = C.c_double(), C.c_double(), C.c_int64()
+        check(lib().lpm_farfield_timing(self._h, int(bool(enable)), C.byref(a), C.byref(b),
+                                        C.byref(n)))
+        return a.value, b.value, n.value
+
     def close(self) -> None:
         if self._h:
             lib().lpm_farfield_destroy(self._h)
@@ -93,6 +101,18 @@ class FarField:
             self.close()
         except Exception:
             pass
+
+
+def octree_stats(src_xyz: np.ndarray, tgt_xyz: np.ndarray, leaf_max: int = 64) -> dict:
+    """Host-only summary of the octree and target blocks (no GPU needed)."""
+    s = np.ascontiguousarray(src_xyz, np.float64)
+    t = np.ascontiguousarray(tgt_xyz, np.float64)
+    out = np.zeros(9, np.int64)
+    check(lib().lpm_octree_stats(s.ctypes.data, s.shape[0], t.ctypes.data if t.size else None,
+                                 t.shape[0], int(leaf_max), out.ctypes.data))
+    keys = ["cells", "leaves", "max_leaf", "max_level", "blocks", "min_block_fill",
+            "targets_covered", "sources_in_leaves", "errors"]
+    return dict(zip(keys, (int(v) for v in out)))
 
 
 def tc_selftest(ctx, A, B, N: int, K: int, a_mn: bool, b_mn: bool):
@@ -112,4 +132,4 @@ def split_weights(w: np.ndarray) -> tuple[np.ndarray, np.ndarray, np.ndarray, np
             w[c:].reshape(16, 128))
 
 
-__all__ = ["FarField", "tc_selftest", "split_weights", "NPARAM", "NNORM", "NIN"]
+__all__ = ["FarField", "octree_stats", "tc_selftest", "split_weights", "NPARAM", "NNORM", "NIN"]

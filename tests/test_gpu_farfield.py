@@ -128,7 +128,7 @@ def test_direct_sum_fallback(gpu_ctx, oracle):
 
     vx, fx, fa, fm, fz = _mesh(5)
     eps = 0.01
-    ff = FarField(theta=0.02, ctx=gpu_ctx)
+    ff = FarField(theta=0.02, rho_min=0.01, ctx=gpu_ctx)
     u = _ff_velocity(ff, vx, fx, fz, fa, fm, eps)
     assert ff.stats()["fallback_blocks"] > 0
     ref = _direct(oracle, vx, fx, fz, fa, fm, eps)
@@ -141,8 +141,8 @@ def test_learned_correction_gains(gpu_ctx, oracle):
     from lpm_gb300.farfield import FarField
 
     ff = FarField(theta=0.5, ctx=gpu_ctx)
-    loss = ff.train(nsamples=1 << 19, epochs=3, batch=8192, lr=2e-3, seed=11, level_min=4,
-                    level_max=6, eps=0.01)
+    loss = ff.train(nsamples=1 << 21, epochs=4, batch=8192, lr=2e-3, seed=11, level_min=4,
+                    level_max=7, eps=0.01)
     assert all(np.isfinite(loss)) and loss[-1] < loss[0]
     vx, fx, fa, fm, fz = _mesh(6)
     eps = 0.01
