@@ -32,6 +32,8 @@ namespace lpm {
 
 namespace {
 
+__constant__ ff::CplxTable kCplx = ff::make_cplx_table();
+
 __global__ void k_ff_sort_src(const double4* __restrict__ src, const int* __restrict__ perm,
                               int64_t n, float4* __restrict__ ys) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
@@ -138,71 +140,52 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
   }
   block_sum128<35>(M, sh);
   const double h = block_max128(hmax, sh);
-  if (t != 0) return;
+  // record: every thread holds the reduced moments; the fields are written
+  // by different threads
   float* r = cd + int64_t(cell) * kCellF;
-  for (int k = 0; k < kCellF; ++k) r[k] = 0.f;
-  r[0] = cf[0], r[1] = cf[1], r[2] = cf[2];
-  r[3] = float(cn);
-  r[4] = float(h);
-  r[5] = float(a[3]);
-  r[6] = float(a[4]);
-  r[7] = float(n);
-  for (int k = 0; k < 9; ++k) r[8 + k] = qf[k];
-  for (int k = 0; k < 35; ++k) r[kCellM + k] = float(M[k]);
-  // traced moments sum g d^b |d|^2 (|b| <= 2) and sum g |d|^4
-  for (int k = 0; k < 10; ++k) {
-    const int e0 = ff::mono_exp(k, 0), e1 = ff::mono_exp(k, 1), e2 = ff::mono_exp(k, 2);
-    r[kCellN1 + k] = float(M[ff::mono_index(e0 + 2, e1, e2)] + M[ff::mono_index(e0, e1 + 2, e2)] +
-                           M[ff::mono_index(e0, e1, e2 + 2)]);
+  if (t == 0) {
+    r[0] = cf[0], r[1] = cf[1], r[2] = cf[2];
+    r[3] = float(cn);
+    r[4] = float(h);
+    r[5] = float(a[3]);
+    r[6] = float(a[4]);
+    r[7] = float(n);
+    for (int k = 0; k < 9; ++k) r[8 + k] = qf[k];
+    for (int k = 63; k < kCellC; ++k) r[k] = 0.f;
+    for (int k = kCellC + 35; k < kCellF; ++k) r[k] = 0.f;
   }
-  {
-    double s4 = 0;
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        int e[3] = {0, 0, 0};
-        e[i] += 2;
-        e[j] += 2;
-        s4 += M[ff::mono_index(e[0], e[1], e[2])];
-      }
-    r[kCellN2] = float(s4);
+  if (t < 35) r[kCellM + t] = float(M[t]);
+  if (t >= 35 && t < 45) {
+    // traced moments sum g d^b |d|^2, |b| <= 2
+    const int k = t - 35;
+    double v = 0;
+    ff::sfor<10>([&](auto I) {
+      constexpr int i = decltype(I)::value;
+      constexpr int e0 = ff::mono_exp(i, 0), e1 = ff::mono_exp(i, 1), e2 = ff::mono_exp(i, 2);
+      if (i == k)
+        v = M[ff::mono_index(e0 + 2, e1, e2)] + M[ff::mono_index(e0, e1 + 2, e2)] +
+            M[ff::mono_index(e0, e1, e2 + 2)];
+    });
+    r[kCellN1 + k] = float(v);
   }
-  // complex moments: z^p conj(z)^q w^k = sum over terms of u^a v^b w^k
-  const double S = a[3] > 0 ? a[3] : 1.0;
-  int j = 0;
-  for (int k = 0; k <= 4; ++k)
-    for (int nn = 0; nn <= 4 - k; ++nn)
-      for (int p = nn; 2 * p >= nn; --p) {
-        const int qq = nn - p;
-        // coefficients of (u + i v)^p (u - i v)^q over v powers
-        double cre[5] = {1, 0, 0, 0, 0}, cim[5] = {0, 0, 0, 0, 0};
-        int deg = 0;
-        for (int f = 0; f < p + qq; ++f) {
-          const double sg = f < p ? 1.0 : -1.0;  // multiply by (u + sg i v)
-          double nre[5] = {0, 0, 0, 0, 0}, nim[5] = {0, 0, 0, 0, 0};
-          for (int b = 0; b <= deg; ++b) {
-            nre[b] += cre[b];
-            nim[b] += cim[b];
-            nre[b + 1] += -sg * cim[b];
-            nim[b + 1] += sg * cre[b];
-          }
-          deg++;
-          for (int b = 0; b <= deg; ++b) cre[b] = nre[b], cim[b] = nim[b];
-        }
-        double re = 0, im = 0;
-        for (int b = 0; b <= nn; ++b) {
-          const double mv = M[ff::mono_index(nn - b, b, k)];
-          re += cre[b] * mv;
-          im += cim[b] * mv;
-        }
-        const double nrm = S * pow(h > 0 ? h : 1.0, double(nn + k));
-        r[kCellC + j] = float(re / nrm);
-        if (2 * p > nn) {
-          r[kCellC + j + 1] = float(im / nrm);
-          j += 2;
-        } else {
-          j += 1;
-        }
-      }
+  if (t == 45) {
+    // sum g |d|^4
+    r[kCellN2] = float(M[ff::mono_index(4, 0, 0)] + M[ff::mono_index(0, 4, 0)] +
+                       M[ff::mono_index(0, 0, 4)] +
+                       2.0 * (M[ff::mono_index(2, 2, 0)] + M[ff::mono_index(2, 0, 2)] +
+                              M[ff::mono_index(0, 2, 2)]));
+  }
+  if (t >= 64 && t < 64 + 35) {
+    // complex moments normalised by S h^(p+q+k)
+    const int j = t - 64;
+    const double S = a[3] > 0 ? a[3] : 1.0;
+    const double hh = h > 0 ? h : 1.0;
+    double v = 0;
+    for (int m = 0; m < kCplx.nterm[j]; ++m) v += double(kCplx.coef[j][m]) * M[kCplx.idx[j][m]];
+    double nrm = S;
+    for (int e = 0; e < kCplx.deg[j]; ++e) nrm *= hh;
+    r[kCellC + j] = float(v / nrm);
+  }
 }
 
 // One CTA (128 threads) per target block: Morton-ordered FP32 positions and

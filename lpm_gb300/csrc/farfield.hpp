@@ -13,7 +13,7 @@ namespace lpm {
 constexpr int kMaxLeaf = 64;        // largest leaf the kernels stage
 constexpr int kTargetBlock = 128;   // targets per block = rows of one MMA tile
 constexpr int kFarCap = 1024;       // far cells per target block
-constexpr int kNearCap = 384;       // near leaves per target block
+constexpr int kNearCap = 640;       // near leaves per target block
 constexpr int kLearnCap = 1024;     // learned (cell, block) pairs per block
 constexpr int kExactMax = 32;       // accepted cells with fewer points are summed exactly
 

@@ -66,6 +66,57 @@ __device__ __forceinline__ void sfor(F&& f) {
   sfor_impl(f, std::make_integer_sequence<int, N>{});
 }
 
+// Complex moments from the real cell-frame moments: feature j (0..34) is the
+// real or imaginary part of z^p conj(z)^q w^k summed over the points,
+// z = d1 + i d2, w = d3, ordered by k, then n = p + q, then p descending
+// (p >= q; p > q gives Re and Im, p = q only Re).  Expanding
+// (u + i v)^p (u - i v)^q over powers of v gives each part as at most five
+// real moments with integer coefficients; deg[j] = p + q + k.
+struct CplxTable {
+  int idx[35][5];
+  float coef[35][5];
+  int nterm[35];
+  int deg[35];
+};
+constexpr CplxTable make_cplx_table() {
+  CplxTable T{};
+  int j = 0;
+  for (int k = 0; k <= 4; ++k)
+    for (int n = 0; n <= 4 - k; ++n)
+      for (int p = n; 2 * p >= n; --p) {
+        const int q = n - p;
+        double cre[6] = {1, 0, 0, 0, 0, 0}, cim[6] = {0, 0, 0, 0, 0, 0};
+        int deg = 0;
+        for (int f = 0; f < p + q; ++f) {
+          const double sg = f < p ? 1.0 : -1.0;  // times (u + sg i v)
+          double nre[6] = {0, 0, 0, 0, 0, 0}, nim[6] = {0, 0, 0, 0, 0, 0};
+          for (int b = 0; b <= deg; ++b) {
+            nre[b] += cre[b];
+            nim[b] += cim[b];
+            nre[b + 1] += -sg * cim[b];
+            nim[b + 1] += sg * cre[b];
+          }
+          ++deg;
+          for (int b = 0; b <= deg; ++b) cre[b] = nre[b], cim[b] = nim[b];
+        }
+        for (int part = 0; part < (2 * p > n ? 2 : 1); ++part) {
+          int m = 0;
+          for (int b = 0; b <= n; ++b) {
+            const double c = part == 0 ? cre[b] : cim[b];
+            if (c != 0.0) {
+              T.idx[j][m] = mono_index(n - b, b, k);
+              T.coef[j][m] = float(c);
+              ++m;
+            }
+          }
+          T.nterm[j] = m;
+          T.deg[j] = n + k;
+          ++j;
+        }
+      }
+  return T;
+}
+
 // Weighted powers A_b = mult_b a^b of a 3-vector.
 __device__ __forceinline__ void weighted_powers(float a0, float a1, float a2, float* A) {
   float p0[5], p1[5], p2[5];

@@ -55,8 +55,12 @@ constexpr int kSmA2 = kSmA1 + 128 * kHid * 2;
 constexpr int kSmA3 = kSmA2 + 128 * kHid * 2;
 constexpr int kSmDY = kSmA3 + 128 * kHid * 2;
 constexpr int kSmTrain = kSmDY + 128 * kOut * 2;  // 196608
-constexpr int kSmInfCell = kSmA2;                 // inference: X, H = A1, cell record
-constexpr int kSmInfer = kSmInfCell + kCellF * 4 + 512;
+// inference: kInfWG independent warpgroups, each with an activation tile H
+// (its input tile X aliases the start of H: layer 1 reads X before its
+// epilogue writes H) and a cell record
+constexpr int kInfWG = 4;
+constexpr int kInfWGBytes = 128 * kHid * 2 + 512;
+constexpr int kSmInfer = kSmWEnd + kInfWG * kInfWGBytes;  // 215040
 
 // element offsets of the matrices in the BF16 weight image and the FP32
 // master vector (same order)
@@ -125,14 +129,39 @@ __device__ __forceinline__ void dsilu_rows(uint32_t tda, uint32_t tz, int warp, 
   }
 }
 
-__device__ __forceinline__ void write_x_row(unsigned char* sm, int row, const float* f) {
+__device__ __forceinline__ void write_x_row(unsigned char* xbuf, int row, const float* f) {
 #pragma unroll
   for (int j = 0; j < kIn / 8; ++j) {
     uint4 u = make_uint4(tc::pack_bf16(f[8 * j], f[8 * j + 1]), tc::pack_bf16(f[8 * j + 2], f[8 * j + 3]),
                          tc::pack_bf16(f[8 * j + 4], f[8 * j + 5]), tc::pack_bf16(f[8 * j + 6], f[8 * j + 7]));
-    *reinterpret_cast<uint4*>(sm + kSmX + tc::cm_off(row, 8 * j, kIn)) = u;
+    *reinterpret_cast<uint4*>(xbuf + tc::cm_off(row, 8 * j, kIn)) = u;
   }
 }
+
+// Barriers of the 128 threads that own a tile: the whole CTA (training) or
+// one warpgroup with its own named barrier (inference).
+struct CtaSync {
+  __device__ void sync() const { __syncthreads(); }
+  __device__ bool any(bool v) const { return __syncthreads_or(v) != 0; }
+  __device__ bool leader() const { return threadIdx.x == 0; }
+};
+struct WgSync {
+  unsigned id;  // named barrier 1..4, 128 threads
+  __device__ void sync() const { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+  __device__ bool any(bool v) const {
+    unsigned r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(unsigned(v)), "r"(id)
+        : "memory");
+    return r != 0;
+  }
+  __device__ bool leader() const { return (threadIdx.x & 127) == 0; }
+};
 
 __device__ __forceinline__ void load_weights(unsigned char* sm, const uint16_t* wbf) {
   const uint4* s = reinterpret_cast<const uint4*>(wbf);
@@ -140,41 +169,42 @@ __device__ __forceinline__ void load_weights(unsigned char* sm, const uint16_t* 
   for (int i = threadIdx.x; i < kSmWEnd / 16; i += blockDim.x) d[i] = s[i];
 }
 
-// Forward through layers 1-3 for the X tile; activations into a1/a2/a3
-// (inference passes the same buffer three times).  Returns false on a timed
-// out wait (all threads agree).
+// Forward of the X tile (at byte offset xo) through layers 1-3, activations
+// into a1/a2/a3 (inference passes one buffer three times), output layer into
+// TMEM columns tb..tb+15.  Returns false on a timed-out wait (all 128
+// threads agree).
+template <class SYNC>
 __device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t* bar, uint32_t& ph,
-                                        int a1, int a2, int a3) {
-  const int t = threadIdx.x, w = t >> 5;
-  const int in_buf[3] = {kSmX, a1, a2};
+                                        const SYNC& s, int xo, int a1, int a2, int a3) {
+  const int row = threadIdx.x & 127, w = threadIdx.x >> 5;
+  const int in_buf[3] = {xo, a1, a2};
   const int out_buf[3] = {a1, a2, a3};
   const int wts[3] = {kSmW1, kSmW2, kSmW3};
 #pragma unroll 1
   for (int l = 0; l < 3; ++l) {
     tc::fence_smem_async();
     tc::fence_before();
-    __syncthreads();
-    if (t == 0) {
+    s.sync();
+    if (s.leader()) {
       tc::fence_after();
       const int k = l == 0 ? kIn : kHid;
       gemm_kk(tb, sbase(sm, in_buf[l]), k * 16, sbase(sm, wts[l]), k * 16, kID128, k / 16);
       tc::commit(bar);
     }
     const bool ok = wait_mma(bar, ph);
-    if (__syncthreads_or(!ok)) return false;
-    silu_rows(tb, w, sm + out_buf[l], t);
+    if (s.any(!ok)) return false;
+    silu_rows(tb, w, sm + out_buf[l], row);
   }
-  // output layer (N = 16) into columns 0..15
   tc::fence_smem_async();
   tc::fence_before();
-  __syncthreads();
-  if (t == 0) {
+  s.sync();
+  if (s.leader()) {
     tc::fence_after();
     gemm_kk(tb, sbase(sm, a3), kHid * 16, sbase(sm, kSmW4), kHid * 16, kID16, kHid / 16);
     tc::commit(bar);
   }
   const bool ok = wait_mma(bar, ph);
-  return !__syncthreads_or(!ok);
+  return !s.any(!ok);
 }
 
 struct MlpArgs {
@@ -193,81 +223,87 @@ struct MlpArgs {
   int* err;
 };
 
-// Persistent: one CTA per SM pulls target blocks; per block, one tile per
-// learned cell; the correction is accumulated per target in registers.
-__global__ void __launch_bounds__(128, 1) k_ff_mlp(const MlpArgs a) {
+// Persistent, one CTA (512 threads) per SM: four independent warpgroups, each
+// with its own quarter of TMEM (128 columns), mbarrier, named barrier and
+// activation tile, pull target blocks; per block, one tile per learned cell,
+// the correction accumulated per target in registers.  While one warpgroup
+// runs its SiLU epilogue the others keep the tensor core busy.
+__global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar[kInfWG];
   __shared__ uint32_t tslot;
-  __shared__ int blk;
+  __shared__ int blk[kInfWG];
   __shared__ float nrm[2 * kIn + 1];
-  const int t = threadIdx.x, w = t >> 5;
+  const int t = threadIdx.x, w = t >> 5, g = t >> 7, lt = t & 127;
   load_weights(sm, a.wbf);
-  for (int i = t; i < 2 * kIn + 1; i += 128) nrm[i] = a.norm[i];
+  for (int i = t; i < 2 * kIn + 1; i += blockDim.x) nrm[i] = a.norm[i];
   if (t == 0) {
-    mbar_init(&bar, 1);
+    for (int i = 0; i < kInfWG; ++i) mbar_init(&bar[i], 1);
     mbar_fence_init();
   }
-  if (w == 0) tc::tmem_alloc(&tslot, 128);
+  if (w == 0) tc::tmem_alloc(&tslot, 128 * kInfWG);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const uint32_t tb = tslot;
+  const uint32_t tb = tslot + 128u * g;
+  const WgSync s{1u + unsigned(g)};
+  const int ho = kSmWEnd + g * kInfWGBytes;  // H, with X at its start
+  float* cell = reinterpret_cast<float*>(sm + ho + 128 * kHid * 2);
   uint32_t ph = 0;
   bool ok = true;
-  float* cell = reinterpret_cast<float*>(sm + kSmInfCell);
   const float oscale = nrm[2 * kIn];
   for (;;) {
-    __syncthreads();
-    if (t == 0) blk = atomicAdd(a.counter, 1);
-    __syncthreads();
-    const int64_t b = blk;
+    s.sync();
+    if (lt == 0) blk[g] = atomicAdd(a.counter, 1);
+    s.sync();
+    const int64_t b = blk[g];
     if (b >= a.nblocks) break;
     const int4 nc = a.cnt[b];
     if (nc.w || nc.z == 0) continue;
-    const float4 x = a.xt[b * kTargetBlock + t];
+    const float4 x = a.xt[b * kTargetBlock + lt];
     float acc[3] = {0.f, 0.f, 0.f};
     for (int k = 0; k < nc.z && ok; ++k) {
       const int c = a.lrn[b * kLearnCap + k];
-      __syncthreads();
-      for (int i = t; i < kCellF; i += 128) cell[i] = a.cd[int64_t(c) * kCellF + i];
-      __syncthreads();
+      s.sync();
+      if (lt < kCellF / 4)
+        reinterpret_cast<float4*>(cell)[lt] = reinterpret_cast<const float4*>(a.cd + int64_t(c) * kCellF)[lt];
+      s.sync();
       float d[3];
       ff::to_cell(cell, x.x, x.y, x.z, d);
-      const ff::PairGeo g = ff::pair_geo(cell, d);
-      const bool use = x.w > 0.f && g.rho >= a.rho_min && g.rho <= 1.f;
+      const ff::PairGeo pg = ff::pair_geo(cell, d);
+      const bool use = x.w > 0.f && pg.rho >= a.rho_min && pg.rho <= 1.f;
       float f[kIn];
-      ff::pair_features(cell, g, a.eps, f);
+      ff::pair_features(cell, pg, a.eps, f);
       f[kBiasIn] = 1.f;
 #pragma unroll
       for (int i = kBiasIn + 1; i < kIn; ++i) f[i] = 0.f;
 #pragma unroll
       for (int i = 0; i < kIn; ++i) f[i] = (f[i] - nrm[i]) * nrm[kIn + i];
-      write_x_row(sm, t, f);
-      ok = forward(sm, tb, &bar, ph, kSmA1, kSmA1, kSmA1);
+      write_x_row(sm + ho, lt, f);
+      ok = forward(sm, tb, &bar[g], ph, s, ho, ho, ho, ho);
       if (!ok) break;
       float o[16];
       tc::ld16(tc::lane_addr(tb, w, 0), o);
       if (use) {
         float dw[3];
-        ff::correction(cell, g, o, oscale, x.x, x.y, x.z, dw);
+        ff::correction(cell, pg, o, oscale, x.x, x.y, x.z, dw);
         acc[0] += dw[0];
         acc[1] += dw[1];
         acc[2] += dw[2];
       }
     }
     if (!ok) break;
-    const int64_t tt = a.tslot[b * kTargetBlock + t];
+    const int64_t tt = a.tslot[b * kTargetBlock + lt];
     if (tt >= 0) {
       a.wout[tt] += acc[0];
       a.wout[a.wstride + tt] += acc[1];
       a.wout[2 * a.wstride + tt] += acc[2];
     }
   }
-  if (!ok && t == 0) atomicExch(a.err, 1);
+  if (!ok && lt == 0) atomicExch(a.err, 1);
   tc::fence_before();
   __syncthreads();
-  if (w == 0) tc::tmem_dealloc(tb, 128);
+  if (w == 0) tc::tmem_dealloc(tslot, 128 * kInfWG);
 }
 
 // ---------------------------------------------------------------------------
@@ -282,7 +318,8 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 __device__ __forceinline__ double unif(uint64_t h) { return double(h >> 11) * (1.0 / 9007199254740992.0); }
 
 // One CTA (128 threads) per job (cell, tile): 128 random targets on the unit
-// sphere with h/|x - c| uniform in [rho_min, theta]; the exact FP64 chord
+// sphere at h/|x - c| in [rho_min, theta] (half of them in the top 30% of the
+// range); the exact FP64 chord
 // sum over the cell's points minus the FP32 order-4 expansion is the
 // residual velocity, stored in the target's canonical frame and normalised.
 __global__ void __launch_bounds__(128) k_ff_samples(const float* __restrict__ cd,
@@ -300,9 +337,12 @@ __global__ void __launch_bounds__(128) k_ff_samples(const float* __restrict__ cd
   const float* cell = cd + int64_t(c) * kCellF;
   const int4 ci = cells[c];
   const uint64_t h0 = mix64(seed ^ mix64(uint64_t(job) * 131 + t));
-  const double u1 = unif(h0), u2 = unif(mix64(h0));
+  const double u1 = unif(h0), u2 = unif(mix64(h0)), u3 = unif(mix64(h0 + 1));
   const double h = cell[4], cn = cell[3];
-  const double rho = rho_min + (theta - rho_min) * u1;
+  // half the targets uniform in rho over [rho_min, theta], half in the top
+  // 30% of the range, where the residual (~ rho^5) and the error are largest
+  const double lo = u3 < 0.5 ? rho_min : theta - 0.3 * (theta - rho_min);
+  const double rho = lo + (theta - lo) * u1;
   const double D = h / rho;
   double ca = cn > 0 ? (1.0 + cn * cn - D * D) / (2.0 * cn) : 0.0;
   ca = fmin(1.0, fmax(-1.0, ca));
@@ -449,7 +489,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(const TrainArgs a) {
   tc::fence_after();
   const uint32_t tb = tslot, T0 = tb, T1 = tb + 128, T2 = tb + 256;
   uint32_t ph = 0;
-  bool ok = forward(sm, tb, &bar, ph, kSmA1, kSmA2, kSmA3);
+  bool ok = forward(sm, tb, &bar, ph, CtaSync{}, kSmX, kSmA1, kSmA2, kSmA3);
   float* g = a.gpart + int64_t(blockIdx.x) * kNParam;
   float loss = 0.f;
   if (ok) {
@@ -704,7 +744,7 @@ void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int6
   a.counter = d.counter;
   a.err = ctx.d_err;
   const int grid = int(std::min<int64_t>(d.nblocks, ctx.num_sms));
-  k_ff_mlp<<<grid, 128, kSmInfer, ctx.stream>>>(a);
+  k_ff_mlp<<<grid, 128 * kInfWG, kSmInfer, ctx.stream>>>(a);
   ctx.launches++;
   LPM_CUDA(cudaGetLastError());
 }
