@@ -687,10 +687,19 @@ def run_c5(args, device):
     # ---- network: trained here on the GPU (not in the timed region) ----------
     ff = FarField(theta=0.5, leaf_max=64, rho_min=0.15, ctx=ctx)
     t0 = time.perf_counter()
-    loss = ff.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
-                    seed=20261203, level_min=5, level_max=8, eps=EPS)
+    if args.ff_weights:
+        saved = np.load(args.ff_weights)
+        ff.set_weights(saved["w"], saved["norm"])
+        ff.set_network(True)
+        loss = [float(x) for x in saved["loss"]] if "loss" in saved else []
+    else:
+        loss = ff.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
+                        seed=20261203, level_min=5, level_max=8, eps=EPS)
     torch.cuda.synchronize(device)
     train_s = time.perf_counter() - t0
+    if args.ff_save:
+        wv, nv_ = ff.get_weights()
+        np.savez(args.ff_save, w=wv, norm=nv_, loss=np.array(loss))
     # ---- one evaluation: learned / expansion only vs the GPU FP64 direct sum --
     xall = torch.cat([st0.vx, st0.fx[st0.fm == 0]])
     rng = np.random.default_rng(20261203)
@@ -778,9 +787,10 @@ def run_c5(args, device):
                                    "correction", "vertices": nv, "leaf_faces": nleaf,
                        "direct_equivalent_interactions_per_step": 4 * ipe,
                        "l2": "flushed between timed steps (512 MiB write)",
-                       "training": {"samples": args.ff_samples, "epochs": args.ff_epochs,
-                                    "batch": 16384, "seconds": round(train_s, 2),
-                                    "loss_per_epoch": [round(float(x), 6) for x in loss]}},
+                       "training": ({"loaded": str(args.ff_weights)} if args.ff_weights else
+                                    {"samples": args.ff_samples, "epochs": args.ff_epochs,
+                                     "batch": 16384, "seconds": round(train_s, 2),
+                                     "loss_per_epoch": [round(float(x), 6) for x in loss]})},
             "speedup_vs_gpu_fp64_direct": round(fp64_eval_s / (step_s / 4), 1),
             "fp64_direct": {"seconds_per_evaluation": round(fp64_eval_s, 3),
                             "value": round(ipe / fp64_eval_s / 1e9, 3),
@@ -812,7 +822,10 @@ def main():
                          "c3: planar dipoles; c4: 256-problem ensemble; "
                          "c5: level 8 on the learned octree far field")
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
-    ap.add_argument("--ff-epochs", type=int, default=6)
+    ap.add_argument("--ff-epochs", type=int, default=16)
+    ap.add_argument("--ff-save", default=None, help="c5: save the trained network (.npz)")
+    ap.add_argument("--ff-weights", default=None,
+                    help="c5: load a saved network instead of training")
     ap.add_argument("--plane-level", type=int, default=9)
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--cpu-targets", type=int, default=8192)

@@ -81,15 +81,22 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
   if (cell >= ncells) return;
   const int4 ci = cells[cell];
   const int s0 = ci.x, n = ci.y, t = threadIdx.x;
-  // pass 1: centre, S, sum g
+  // pass 1: centre, S, sum g (FP32 per 32-point batch per thread, FP64 across
+  // batches: the FP64 pipe is 1/64 of FP32 on this part)
   double a[5] = {0, 0, 0, 0, 0};
-  for (int i = t; i < n; i += 128) {
-    const float4 p = ys[s0 + i];
-    a[0] += p.x;
-    a[1] += p.y;
-    a[2] += p.z;
-    a[3] += fabs((double)p.w);
-    a[4] += p.w;
+  for (int b0 = 0; b0 < n; b0 += 128 * 32) {
+    float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const int e = min(n, b0 + 128 * 32);
+    for (int i = b0 + t; i < e; i += 128) {
+      const float4 p = ys[s0 + i];
+      f[0] += p.x;
+      f[1] += p.y;
+      f[2] += p.z;
+      f[3] += fabsf(p.w);
+      f[4] += p.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) a[k] += f[k];
   }
   block_sum128<5>(a, sh);
   const double c[3] = {a[0] / n, a[1] / n, a[2] / n};
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
   double M[35];
 #pragma unroll
   for (int k = 0; k < 35; ++k) M[k] = 0.0;
-  double hmax = 0.0;
+  float hmax = 0.f;
   for (int b0 = 0; b0 < n; b0 += 128 * 32) {
     float m[35];
 #pragma unroll
@@ -125,7 +132,7 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
       const float d0 = qf[0] * x0 + qf[1] * x1 + qf[2] * x2;
       const float d1 = qf[3] * x0 + qf[4] * x1 + qf[5] * x2;
       const float d2 = qf[6] * x0 + qf[7] * x1 + qf[8] * x2;
-      hmax = fmax(hmax, (double)sqrtf(d0 * d0 + d1 * d1 + d2 * d2));
+      hmax = fmaxf(hmax, d0 * d0 + d1 * d1 + d2 * d2);
       float p0[5], p1[5], p2[5];
       p0[0] = p1[0] = p2[0] = 1.f;
 #pragma unroll
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
     for (int k = 0; k < 35; ++k) M[k] += m[k];
   }
   block_sum128<35>(M, sh);
-  const double h = block_max128(hmax, sh);
+  const double h = sqrt(block_max128(double(hmax), sh));
   // record: every thread holds the reduced moments; the fields are written
   // by different threads
   float* r = cd + int64_t(cell) * kCellF;

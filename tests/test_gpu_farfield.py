@@ -141,19 +141,19 @@ def test_learned_correction_gains(gpu_ctx, oracle):
     from lpm_gb300.farfield import FarField
 
     ff = FarField(theta=0.5, ctx=gpu_ctx)
-    loss = ff.train(nsamples=1 << 21, epochs=4, batch=8192, lr=2e-3, seed=11, level_min=4,
-                    level_max=7, eps=0.01)
+    loss = ff.train(nsamples=1 << 22, epochs=6, batch=16384, lr=2e-3, seed=11, level_min=5,
+                    level_max=8, eps=0.01)
     assert all(np.isfinite(loss)) and loss[-1] < loss[0]
-    vx, fx, fa, fm, fz = _mesh(6)
+    vx, fx, fa, fm, fz = _mesh(7)
     eps = 0.01
-    x = vx[::4]
+    x = vx[::8]
     ref = _direct(oracle, x, fx, fz, fa, fm, eps)
     ff.set_network(False)
     e0 = _rel_linf(_ff_velocity(ff, x, fx, fz, fa, fm, eps), ref)
     ff.set_network(True)
     e1 = _rel_linf(_ff_velocity(ff, x, fx, fz, fa, fm, eps), ref)
     assert ff.stats()["learned_tiles"] > 0
-    assert e1 < 0.8 * e0, (e0, e1)
+    assert e1 < 0.6 * e0, (e0, e1)
     # weights round-trip through the host
     w, nrm = ff.get_weights()
     ff2 = FarField(theta=0.5, ctx=gpu_ctx)
