@@ -677,7 +677,15 @@ def run_c5(args, device):
     stream = torch.cuda.current_stream(device)
     ctx.set_stream(stream)
     L = args.level if args.level != LEVEL else 8
+    t0 = time.perf_counter()
     vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, L, 1.0)
+    mesh_host_s = time.perf_counter() - t0
+    core.build_mesh_device(ctx, core.MESH_ICOS_TRI, L)  # warm
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    core.build_mesh_device(ctx, core.MESH_ICOS_TRI, L)
+    torch.cuda.synchronize(device)
+    mesh_dev_s = time.perf_counter() - t0
     w = OMEGA / 12.5
     vz = core.eval_ic(core.IC_RH54, (w, -w), vx)
     fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
@@ -685,7 +693,7 @@ def run_c5(args, device):
     ipe = (nv + nleaf) * nleaf
     st0 = DeviceState((vx, fx, fa, fm, vz, fz), device)
     # ---- network: trained here on the GPU (not in the timed region) ----------
-    ff = FarField(theta=0.5, leaf_max=64, rho_min=0.15, ctx=ctx)
+    ff = FarField(theta=0.5, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
     t0 = time.perf_counter()
     if args.ff_weights:
         saved = np.load(args.ff_weights)
@@ -784,13 +792,14 @@ def run_c5(args, device):
                                           "network trained on seeded random vortex fields)",
             "config": {"workload": f"BVE sphere icosahedral level {L} RK4, RH R=4, eps={EPS}, "
                                    f"dt={DT}, octree far field theta=0.5 leaf<=64 + learned "
-                                   "correction", "vertices": nv, "leaf_faces": nleaf,
+                                   f"correction for rho >= {args.ff_rho_min}", "vertices": nv, "leaf_faces": nleaf,
                        "direct_equivalent_interactions_per_step": 4 * ipe,
                        "l2": "flushed between timed steps (512 MiB write)",
                        "training": ({"loaded": str(args.ff_weights)} if args.ff_weights else
                                     {"samples": args.ff_samples, "epochs": args.ff_epochs,
                                      "batch": 16384, "seconds": round(train_s, 2),
                                      "loss_per_epoch": [round(float(x), 6) for x in loss]})},
+            "mesh_build_seconds": {"host": round(mesh_host_s, 3), "device": round(mesh_dev_s, 4)},
             "speedup_vs_gpu_fp64_direct": round(fp64_eval_s / (step_s / 4), 1),
             "fp64_direct": {"seconds_per_evaluation": round(fp64_eval_s, 3),
                             "value": round(ipe / fp64_eval_s / 1e9, 3),
@@ -823,6 +832,8 @@ def main():
                          "c5: level 8 on the learned octree far field")
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
+    ap.add_argument("--ff-rho-min", type=float, default=0.15,
+                    help="c5: learned correction for cells with h/(D - r_block) >= this")
     ap.add_argument("--ff-save", default=None, help="c5: save the trained network (.npz)")
     ap.add_argument("--ff-weights", default=None,
                     help="c5: load a saved network instead of training")

@@ -281,6 +281,12 @@ int lpm_mesh_sizes(int kind, int level, int64_t* nverts, int64_t* nfaces);
 int lpm_mesh_build(int kind, int level, double radius, double* vx, double* fx,
                    double* farea, uint8_t* fmask);
 
+/* The same mesh built on the device (uniform refinement in parallel, one
+ * level per pass): DEVICE arrays of lpm_mesh_sizes' sizes.  Positions equal
+ * lpm_mesh_build's bit for bit; areas to the last bits of tan/atan. */
+int lpm_mesh_build_device(lpm_context* ctx, int kind, int level, double radius,
+                          double* vx, double* fx, double* farea, uint8_t* fmask);
+
 /* Initial vorticity kinds (src/lpm_vorticity_gallery.hpp). */
 #define LPM_IC_SOLID_BODY 1      /* SolidBodyRotation: 2*OMEGA*z, OMEGA=2pi */
 #define LPM_IC_GAUSSIAN_SPHERE 2 /* params: strength, b, lon, lat, gauss_const,

@@ -21,7 +21,7 @@ LIB = OUT / "liblpm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "ensemble.cu", "farfield.cu",
-              "mlp.cu", "ffapi.cu"]
+              "mlp.cu", "ffapi.cu", "mesh_dev.cu"]
 CXX_SOURCES = ["mesh.cpp", "ics.cpp", "tree.cpp"]
 
 
@@ -64,7 +64,10 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         o = OUT / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", *inc, "-c", str(s), "-o", str(o)])
+            # no contraction: the same FP64 results on x86-64 and aarch64 hosts,
+            # and the on-device mesh generator reproduces the host mesh bitwise
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
+                         str(s), "-o", str(o)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for cmd in jobs:

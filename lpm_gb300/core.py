@@ -62,7 +62,7 @@ EXPORTS = [
     "lpm_farfield_create", "lpm_farfield_destroy", "lpm_farfield_velocity", "lpm_farfield_train",
     "lpm_farfield_set_network", "lpm_farfield_get_weights", "lpm_farfield_set_weights",
     "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
-    "lpm_octree_stats",
+    "lpm_octree_stats", "lpm_mesh_build_device",
 ]
 
 
@@ -153,6 +153,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_tc_selftest": [vp, vp, vp, vp, i32, i32, i32, i32],
         "lpm_farfield_timing": [vp, i32, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)],
         "lpm_octree_stats": [vp, i64, vp, i64, i32, vp],
+        "lpm_mesh_build_device": [vp, i32, i32, dbl, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -259,6 +260,22 @@ def build_mesh(kind: int, level: int, radius: float = 1.0):
     fa = np.empty(nf, np.float64)
     fm = np.empty(nf, np.uint8)
     check(lib().lpm_mesh_build(kind, level, radius, ptr(vx), ptr(fx), ptr(fa), ptr(fm)))
+    return vx, fx, fa, fm
+
+
+def build_mesh_device(ctx, kind: int, level: int, radius: float = 1.0):
+    """The same mesh built on the context's GPU: torch tensors (vx, fx, farea, fmask)."""
+    import torch
+
+    nv, nf = mesh_sizes(kind, level)
+    ndim = 2 if kind == MESH_QUAD_RECT else 3
+    dev = torch.device("cuda", ctx.device)
+    vx = torch.empty((nv, ndim), dtype=torch.float64, device=dev)
+    fx = torch.empty((nf, ndim), dtype=torch.float64, device=dev)
+    fa = torch.empty(nf, dtype=torch.float64, device=dev)
+    fm = torch.empty(nf, dtype=torch.uint8, device=dev)
+    check(lib().lpm_mesh_build_device(ctx.handle, kind, level, radius, vx.data_ptr(),
+                                      fx.data_ptr(), fa.data_ptr(), fm.data_ptr()))
     return vx, fx, fa, fm
 
 

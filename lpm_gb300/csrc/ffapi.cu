@@ -301,6 +301,21 @@ int lpm_octree_stats(const double* src_xyz, int64_t nsrc, const double* tgt_xyz,
   }
 }
 
+int lpm_mesh_build_device(lpm_context* ctx, int kind, int level, double radius, double* vx,
+                          double* fx, double* farea, uint8_t* fmask) {
+  if (!ctx || !vx || !fx || !farea || !fmask) return fail(LPM_ERR_ARG, "null argument");
+  if (kind < LPM_MESH_ICOS_TRI || kind > LPM_MESH_QUAD_RECT) return fail(LPM_ERR_ARG, "unknown mesh kind");
+  if (level < 0 || level > 10) return fail(LPM_ERR_ARG, "mesh level out of range [0, 10]");
+  if (!(radius > 0) || !std::isfinite(radius)) return fail(LPM_ERR_ARG, "radius must be positive");
+  try {
+    cudaSetDevice(ctx->device);
+    lpm::mesh_build_device(*ctx, kind, level, radius, vx, fx, farea, fmask);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
 int lpm_tc_selftest(lpm_context* ctx, const float* A, const float* B, float* D, int N, int K,
                     int a_mn, int b_mn) {
   if (!ctx || !A || !B || !D) return fail(LPM_ERR_ARG, "null argument");

@@ -6,6 +6,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "lpm_gb300.h"
 
@@ -17,6 +18,14 @@ void mesh_build(int kind, int level, double radius, double* vx, double* fx,
                 double* farea, uint8_t* fmask);
 void ic_eval(int kind, const double* prm, int np, int ndim, int64_t n,
              const double* x, double* zeta);
+// Level-0 mesh (the seed) with its face vertex lists (nfv per face).
+struct MeshSeed {
+  int ndim = 3, nfv = 3;
+  bool sphere = true;
+  std::vector<double> vx, fx, area;
+  std::vector<int> fverts;
+};
+void mesh_seed(int kind, double radius, MeshSeed& out);
 
 // An error carrying an lpm status code; the C ABI turns it into a return
 // code plus the thread-local message.
@@ -185,6 +194,9 @@ void invariants(lpm_context& ctx, int ndim, int64_t n, const double* zeta,
 void err_norms(lpm_context& ctx, int ndim, int64_t n, View appx, View exact,
                const double* wt, const uint8_t* mask, double out[3]);
 double fma_peak(lpm_context& ctx, int precision);
+// Uniform mesh built on the device (mesh_dev.cu); device output arrays.
+void mesh_build_device(lpm_context& ctx, int kind, int level, double radius, double* vx,
+                       double* fx, double* farea, uint8_t* fmask);
 void check_device_error(lpm_context& ctx);
 
 }  // namespace lpm

@@ -306,6 +306,32 @@ void mesh_sizes(int kind, int level, int64_t* nv, int64_t* nf) {
   *nf = total;
 }
 
+void mesh_seed(int kind, double radius, MeshSeed& out) {
+  Builder b;
+  switch (kind) {
+    case LPM_MESH_ICOS_TRI:
+      seed_icosahedron(b);
+      break;
+    case LPM_MESH_CUBED_SPHERE:
+      seed_cube(b);
+      break;
+    case LPM_MESH_QUAD_RECT:
+      seed_square(b, radius);
+      break;
+    default:
+      throw std::invalid_argument("unknown mesh kind");
+  }
+  out.ndim = b.ndim;
+  out.nfv = b.nfv;
+  out.sphere = b.sphere;
+  out.vx = b.vx;
+  out.fx = b.fx;
+  out.area = b.area;
+  out.fverts.clear();
+  for (const auto& f : b.fverts)
+    for (int i = 0; i < b.nfv; ++i) out.fverts.push_back(int(f[i]));
+}
+
 void mesh_build(int kind, int level, double radius, double* vx, double* fx,
                 double* farea, uint8_t* fmask) {
   int64_t nv, nf;

@@ -6,9 +6,9 @@
 // (canonical frame, normalised by S rho^5 / (2 pi D)).  48 -> 128 -> 128 ->
 // 128 -> 16, SiLU, BF16 weights and activations, FP32 accumulation in TMEM.
 //
-// SiLU runs on packed BF16 pairs (h = z/2, t = tanh.approx.bf16x2(h),
-// h t + h): the special-function unit, not the tensor core, bounds the
-// epilogue, and this halves its work.
+// The epilogue's SiLU (one tanh.approx.f32 per activation) keeps the
+// special-function unit busier than the tensor core: it, not the MMA, bounds
+// the inference kernel (packed BF16 tanh measured no faster on this part).
 //
 // Tile = 128 rows (one target block against one cell at inference, 128
 // training samples in training) x one layer: tcgen05.mma with M = 128,
@@ -93,17 +93,6 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
   return ok;
 }
 
-// SiLU of two values on packed BF16: h = z/2, t = tanh(h), silu = h t + h
-// (one special-function instruction per pair; the result is the next
-// layer's operand).
-__device__ __forceinline__ uint32_t silu_bf16x2(float a, float b) {
-  const uint32_t h = tc::pack_bf16(0.5f * a, 0.5f * b);
-  uint32_t t, r;
-  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
-  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(r) : "r"(h), "r"(t));
-  return r;
-}
-
 // Bias + SiLU epilogue of one 128-column layer: TMEM lane row -> BF16 row of
 // the next operand (unit kBiasHid is the constant 1).
 __device__ __forceinline__ void silu_rows(uint32_t tacc, int warp, unsigned char* dst, int row) {
@@ -114,8 +103,9 @@ __device__ __forceinline__ void silu_rows(uint32_t tacc, int warp, unsigned char
     uint32_t p[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      p[i] = silu_bf16x2(v[2 * i], v[2 * i + 1]);
-      if (cc + 2 * i + 1 == kBiasHid) p[i] = (p[i] & 0xFFFFu) | (0x3F80u << 16);  // BF16 1.0
+      float a = ff::silu(v[2 * i]), b = ff::silu(v[2 * i + 1]);
+      if (cc + 2 * i + 1 == kBiasHid) b = 1.f;
+      p[i] = tc::pack_bf16(a, b);
     }
     *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc, kHid)) = make_uint4(p[0], p[1], p[2], p[3]);
     *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);

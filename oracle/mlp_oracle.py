@@ -3,8 +3,7 @@ network's forward pass and gradient, with BF16 rounding at the same points as
 the tensor-core kernels (lpm_gb300/csrc/mlp.cu), so the GPU gradient can be
 checked against it.  Imported by tests only; never by the product path.
 
-Network: 48 inputs -> 128 -> 128 -> 128 -> 16 (first 3 outputs used), SiLU
-(evaluated on packed BF16 in the forward pass, FP32 derivative backward).
+Network: 48 inputs -> 128 -> 128 -> 128 -> 16 (first 3 outputs used), SiLU.
 Input 40 and hidden unit 127 of every layer are the constant 1 (the next
 weight matrix's column that multiplies them is the bias).  Loss: mean over the
 n rows of the summed squared error of the 3 outputs.
@@ -35,15 +34,6 @@ def silu(z):
     return z / (1.0 + np.exp(-z))
 
 
-def silu_bf16(z):
-    """SiLU as the kernels evaluate it on packed BF16: h = bf16(z/2),
-    t = bf16(tanh(h)), silu = bf16(h t + h) (one rounding of the fused
-    multiply-add)."""
-    h = bf16(0.5 * np.asarray(z, np.float64))
-    t = bf16(np.tanh(h))
-    return bf16(h * t + h)
-
-
 def silu_grad(z):
     s = 1.0 / (1.0 + np.exp(-z))
     return s * (1.0 + z * (1.0 - s))
@@ -56,14 +46,13 @@ def forward(w, x, rounding=True):
     W1, W2, W3, W4 = (r(m) for m in split(w))
     X = r(x)
     Z1 = X @ W1.T
-    act = silu_bf16 if rounding else silu
-    A1 = act(Z1)
+    A1 = r(silu(Z1))
     A1[:, BIAS_HID] = 1.0
     Z2 = A1 @ W2.T
-    A2 = act(Z2)
+    A2 = r(silu(Z2))
     A2[:, BIAS_HID] = 1.0
     Z3 = A2 @ W3.T
-    A3 = act(Z3)
+    A3 = r(silu(Z3))
     A3[:, BIAS_HID] = 1.0
     Y = A3 @ W4.T
     return Y, (X, Z1, A1, Z2, A2, Z3, A3, W1, W2, W3, W4)

@@ -153,7 +153,7 @@ def test_learned_correction_gains(gpu_ctx, oracle):
     ff.set_network(True)
     e1 = _rel_linf(_ff_velocity(ff, x, fx, fz, fa, fm, eps), ref)
     assert ff.stats()["learned_tiles"] > 0
-    assert e1 < 0.6 * e0, (e0, e1)
+    assert e1 < 0.8 * e0, (e0, e1)
     # weights round-trip through the host
     w, nrm = ff.get_weights()
     ff2 = FarField(theta=0.5, ctx=gpu_ctx)
