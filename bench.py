@@ -173,6 +173,17 @@ def advance(h, st):
         ptr(st.fa), ptr(st.fm)))
 
 
+def fp32_peak(device) -> tuple[float, float, int]:
+    """Computed FP32 FMA peak (TFLOP/s) 2*128*SMs*sm_max_mhz, with sm_max_mhz and SMs."""
+    import torch
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    return 2 * 128 * nsm * sm_max * 1e6 / 1e12, sm_max, nsm
+
+
 def rel_errors(got, ref, mask=None):
     import torch
 
@@ -494,6 +505,8 @@ def run_ensemble(args, device):
     clocks = sampler.stop()
     launches = ctx.kernel_launches - l0
     info = ens.info()
+    peak, sm_max, nsm = fp32_peak(device)
+    ach = 4 * ipe * args.steps * FLOPS_PER_PAIR / (ms * 1e-3) / 1e12
     return {"metric": METRIC, "value": round(4 * ipe * args.steps / (ms * 1e-3) / 1e9, 3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
@@ -504,6 +517,11 @@ def run_ensemble(args, device):
                        "levels_histogram": {int(l): int((levels == l).sum()) for l in range(3, 7)},
                        "interactions_per_step": 4 * ipe, "chunk_len": info["chunk_len"],
                        "work_items_per_evaluation": info["items"], "autotune_s": round(tune_s, 2)},
+            "roofline": {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2),
+                         "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
+                         "kernel": "ensemble N-body (persistent), whole RK4 step timed",
+                         "flops_per_pair_credited": FLOPS_PER_PAIR,
+                         "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"},
             "clocks": clocks, "gpu_launches": launches}
 
 
@@ -577,6 +595,21 @@ def run_c1(args, device):
             "gpu_launches": launches}
 
 
+def c3_roofline(device, pairs_per_s: float) -> dict:
+    """Planar u + psi: 16 credited flops per pair against the FP32 FMA peak;
+    the pair needs two special-function results (reciprocal, log2), so the
+    XU pipe (16 per clock per SM) bounds it at 8 pairs per clock per SM."""
+    peak, sm_max, nsm = fp32_peak(device)
+    ach = pairs_per_s * 16 / 1e12
+    xu_pairs = 8 * nsm * sm_max * 1e6
+    return {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
+            "frac": round(ach / peak, 4), "traffic": None,
+            "kernel": "nbody_chord<float,2,u,psi>, whole RK2 step timed",
+            "flops_per_pair_credited": 16,
+            "xu_bound_pairs_per_s": xu_pairs, "frac_of_xu_bound": round(pairs_per_s / xu_pairs, 4),
+            "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"}
+
+
 def run_plane(args, device):
     """Configuration C3: planar incompressible flow, colliding Lamb dipoles of
     radius 1 and strength +-2 centred at (-+2, 0), uniform quad mesh of
@@ -644,6 +677,7 @@ def run_plane(args, device):
             "config": {"workload": f"planar colliding dipoles, quad level {args.plane_level} on "
                                    "[-4,4]^2, eps=0.02, RK2 dt=0.01", "vertices": nv,
                        "leaf_faces": nleaf, "interactions_per_step": 2 * ipe},
+            "roofline": c3_roofline(device, 2 * ipe * args.steps / (ms * 1e-3)),
             "errors_fp32c_vs_fp64_16384_vertex_targets": err,
             "invariants_after": {"circulation": inv[0], "enstrophy": inv[1],
                                  "kinetic_energy": inv[2]},
@@ -832,7 +866,7 @@ def main():
                          "c5: level 8 on the learned octree far field")
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
-    ap.add_argument("--ff-rho-min", type=float, default=0.15,
+    ap.add_argument("--ff-rho-min", type=float, default=0.2,
                     help="c5: learned correction for cells with h/(D - r_block) >= this")
     ap.add_argument("--ff-save", default=None, help="c5: save the trained network (.npz)")
     ap.add_argument("--ff-weights", default=None,

@@ -92,10 +92,74 @@ class BVERK4 {
     require(lpm_bve_rk4_advance_timestep(h_, vx, vzeta, vvel, fx, fzeta, fvel, farea, fmask),
             "BVERK4::advance_timestep");
   }
+  // evaluate the stages with an octree far field (LPM_FP64_CHORD steppers)
+  void set_farfield(lpm_farfield* ff, int rebuild_every = 0) {
+    require(lpm_bve_rk4_set_farfield(h_, ff, rebuild_every), "BVERK4::set_farfield");
+  }
   double dt, Omega;
 
  private:
   lpm_bve_rk4* h_ = nullptr;
+};
+
+// Octree far field with the learned correction (no reference counterpart).
+class FarField {
+ public:
+  explicit FarField(Context& c, double theta = 0.5, int leaf_max = 64, double rho_min = 0.15) {
+    require(lpm_farfield_create(c.get(), &h_, theta, leaf_max, rho_min), "FarField");
+  }
+  ~FarField() { lpm_farfield_destroy(h_); }
+  FarField(const FarField&) = delete;
+  FarField& operator=(const FarField&) = delete;
+  // trains on the GPU; loss (optional) receives one value per epoch
+  void train(int64_t nsamples, int epochs, int batch, double lr, uint64_t seed, int level_min,
+             int level_max, double eps, float* loss = nullptr) {
+    require(lpm_farfield_train(h_, nsamples, epochs, batch, lr, seed, level_min, level_max, eps,
+                               loss),
+            "FarField::train");
+  }
+  void load(const float* w, const float* norm) {
+    require(lpm_farfield_set_weights(h_, w, norm), "FarField::load");
+  }
+  void save(float* w, float* norm) { require(lpm_farfield_get_weights(h_, w, norm), "FarField::save"); }
+  void set_network(bool on) { require(lpm_farfield_set_network(h_, on ? 1 : 0), "FarField::set_network"); }
+  void velocity(lpm_view u, lpm_view x, int64_t nx, lpm_view fx, const double* zeta,
+                const double* area, const uint8_t* mask, int64_t nf, double eps) {
+    require(lpm_farfield_velocity(h_, u, x, nx, fx, zeta, area, mask, nf, eps),
+            "FarField::velocity");
+  }
+  lpm_farfield* get() { return h_; }
+
+ private:
+  lpm_farfield* h_ = nullptr;
+};
+
+// Many independent BVE problems advanced together (one persistent launch per
+// evaluation, graph-captured steps).
+class BVEEnsemble {
+ public:
+  BVEEnsemble(Context& c, int nproblems, const int64_t* nverts, const int64_t* nfaces,
+              const uint8_t* fmask, double dt, double Omega, double eps,
+              int precision = LPM_FP32C, uint32_t flags = 0) {
+    require(lpm_ensemble_create(c.get(), &h_, nproblems, nverts, nfaces, fmask, dt, Omega, eps,
+                                precision, flags),
+            "BVEEnsemble");
+  }
+  ~BVEEnsemble() { lpm_ensemble_destroy(h_); }
+  BVEEnsemble(const BVEEnsemble&) = delete;
+  BVEEnsemble& operator=(const BVEEnsemble&) = delete;
+  void velocity(lpm_view vx, lpm_view vvel, lpm_view fx, const double* fzeta, lpm_view fvel,
+                const double* farea) {
+    require(lpm_ensemble_velocity(h_, vx, vvel, fx, fzeta, fvel, farea), "BVEEnsemble::velocity");
+  }
+  void advance_timestep(lpm_view vx, double* vzeta, lpm_view vvel, lpm_view fx, double* fzeta,
+                        lpm_view fvel, const double* farea) {
+    require(lpm_ensemble_advance_timestep(h_, vx, vzeta, vvel, fx, fzeta, fvel, farea),
+            "BVEEnsemble::advance_timestep");
+  }
+
+ private:
+  lpm_ensemble* h_ = nullptr;
 };
 
 // ---- Incompressible2DRK2 (src/lpm_incompressible2d_rk2.hpp) --------------
