@@ -305,6 +305,32 @@ int lpm_ic_eval(int kind, const double* params, int nparams, int ndim,
  * register-only microbenchmark; synchronous. */
 int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops);
 
+/* ---- planar shallow-water direct sums ------------------------------------ */
+/* PlanarSWEVertexSums (src/lpm_swe_kernels.hpp:626-721): at nv vertices vx
+ * (nv x 2) with surface height vs, from the face slots fx/fzeta/fsigma/
+ * farea/fmask/fs (nf): velocity u (written if do_velocity), the double dot
+ * product du/dx^2 + 2 du/dy dv/dx + dv/dy^2, the four velocity gradients,
+ * the PSE surface Laplacian (pse::BivariateOrder8 of width pse_eps), the
+ * stream and potential functions.  FP64, the reference's pair arithmetic
+ * (planar_swe_sums_rhs_pse, :394-480); masked faces are skipped. */
+int lpm_swe_plane_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot,
+                              double* du1dx1, double* du1dx2, double* du2dx1,
+                              double* du2dx2, double* laps, double* psi,
+                              double* phi, lpm_view vx, const double* vs,
+                              int64_t nv, lpm_view fx, const double* fzeta,
+                              const double* fsigma, const double* farea,
+                              const uint8_t* fmask, const double* fs, int64_t nf,
+                              double eps, double pse_eps, int do_velocity);
+/* PlanarSWEFaceSums (:787-876): the same at every face slot; for eps == 0 the
+ * i == j pair is skipped (collocated = !(eps > 0)). */
+int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
+                            double* du1dx1, double* du1dx2, double* du2dx1,
+                            double* du2dx2, double* laps, double* psi,
+                            double* phi, lpm_view fx, const double* fzeta,
+                            const double* fsigma, const double* farea,
+                            const uint8_t* fmask, const double* fs, int64_t nf,
+                            double eps, double pse_eps, int do_velocity);
+
 /* ---- octree far field with a learned correction ------------------------- */
 /* No reference counterpart: the reference's octree sources (LpmOctree*,
  * LpmNodeArray*) are not built and src/tree/lpm_cpu_tree's generators are

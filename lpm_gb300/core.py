@@ -62,7 +62,8 @@ EXPORTS = [
     "lpm_farfield_create", "lpm_farfield_destroy", "lpm_farfield_velocity", "lpm_farfield_train",
     "lpm_farfield_set_network", "lpm_farfield_get_weights", "lpm_farfield_set_weights",
     "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
-    "lpm_octree_stats", "lpm_mesh_build_device",
+    "lpm_octree_stats", "lpm_mesh_build_device", "lpm_swe_plane_vertex_sums",
+    "lpm_swe_plane_face_sums",
 ]
 
 
@@ -154,6 +155,10 @@ def _declare(L: C.CDLL) -> None:
         "lpm_farfield_timing": [vp, i32, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(i64)],
         "lpm_octree_stats": [vp, i64, vp, i64, i32, vp],
         "lpm_mesh_build_device": [vp, i32, i32, dbl, vp, vp, vp, vp],
+        "lpm_swe_plane_vertex_sums": [vp, V, vp, vp, vp, vp, vp, vp, vp, vp, V, vp, i64, V, vp, vp,
+                                      vp, vp, vp, i64, dbl, dbl, i32],
+        "lpm_swe_plane_face_sums": [vp, V, vp, vp, vp, vp, vp, vp, vp, vp, V, vp, vp, vp, vp, vp,
+                                    i64, dbl, dbl, i32],
     }
     for name, args in sig.items():
         f = getattr(L, name)

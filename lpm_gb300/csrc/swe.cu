@@ -1,0 +1,260 @@
+// swe.cu -- planar shallow-water direct sums with particle strength exchange
+// (PlanarSWEVertexSums / PlanarSWEFaceSums, src/lpm_swe_kernels.hpp:626-876).
+//
+// Pair term (planar_swe_sums_rhs_pse, :394-480): with d = x - y,
+// R = |d|^2 + eps^2, rot = zeta A, pot = sigma A,
+//   u, v         = (-d1 rot + d0 pot) / (2 pi R), (d0 rot + d1 pot) / (2 pi R)
+//   du/dx, du/dy, dv/dx, dv/dy from pi R^2 and 2 pi R denominators,
+//   lap(s)       = (s_y - s_x) A lapPSE(|y - x| / pse_eps) / pse_eps^2,
+//                  lapPSE(r) = (40 (1 - r^2) + 10 r^4 - 2 r^6 / 3) e^{-r^2} / pi
+//                  (pse::BivariateOrder8::laplacian, src/lpm_pse.hpp:66-72),
+//   psi, phi     = -log(R) / (4 pi) times rot, pot.
+// Reducer rules (:559-570): masked sources are skipped; with collocated
+// targets (face sums with eps = 0) the i == j pair is skipped.
+//
+// FP64 in the reference's operation order with non-contracting intrinsics:
+// every term equals the reference's except through exp/log, whose last bits
+// may differ from the host library's.  One CTA = 128 targets x one chunk of
+// the compacted sources (tiles of 256 in shared memory); FP64 partials per
+// (chunk, component, target) are added in fixed order by the epilogue, which
+// also forms the double dot product du/dx^2 + 2 du/dy dv/dx + dv/dy^2.
+#include <algorithm>
+#include <cmath>
+
+#include <cuda_runtime.h>
+
+#include "lpm_host.hpp"
+#include "nbody.cuh"
+
+namespace lpm {
+int fail(int code, const char* msg);  // capi.cu
+int handle_exception();               // capi.cu
+
+namespace {
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dd(double a, double b) { return __ddiv_rn(a, b); }
+
+constexpr int kSweNT = 128;   // targets per CTA
+constexpr int kSweTile = 256;  // sources per shared-memory tile
+constexpr int kSweNC = 9;
+
+struct SweSrc {
+  double x, y, rot, pot, s, area;
+  int slot, pad;
+};
+
+__global__ void k_swe_pack(View fx, const double* __restrict__ zeta, const double* __restrict__ sigma,
+                           const double* __restrict__ area, const double* __restrict__ sfc,
+                           const int* __restrict__ src2slot, int64_t ns, SweSrc* __restrict__ src) {
+  const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = src2slot[k];
+  SweSrc r;
+  r.x = fx(j, 0);
+  r.y = fx(j, 1);
+  r.rot = dm(zeta[j], area[j]);
+  r.pot = dm(sigma[j], area[j]);
+  r.s = sfc[j];
+  r.area = area[j];
+  r.slot = int(j);
+  r.pad = 0;
+  src[k] = r;
+}
+
+__global__ void __launch_bounds__(kSweNT) k_swe_plane(View tx, const double* __restrict__ ts,
+                                                      int64_t nt, const SweSrc* __restrict__ src,
+                                                      int64_t ns, int64_t chunk_len, double eps,
+                                                      double pse_eps, int collocated,
+                                                      double* __restrict__ part, int64_t tpad) {
+  __shared__ SweSrc tile[kSweTile];
+  const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
+  const bool valid = i < nt;
+  const double x0 = valid ? tx(i, 0) : 0.0, x1 = valid ? tx(i, 1) : 0.0;
+  const double si = valid ? ts[i] : 0.0;
+  const double epssq = dm(eps, eps);
+  const double pse2 = dm(pse_eps, pse_eps);
+  const double twopi = 2 * kPI, fourpi = 4 * kPI;
+  double r[kSweNC];
+#pragma unroll
+  for (int k = 0; k < kSweNC; ++k) r[k] = 0.0;
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+    const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += kSweNT) tile[q] = src[t0 + q];
+    __syncthreads();
+    if (!valid) continue;
+    for (int q = 0; q < m; ++q) {
+      const SweSrc& y = tile[q];
+      if (collocated && y.slot == i) continue;
+      const double d0 = ds(x0, y.x), d1 = ds(x1, y.y);
+      const double rsq = da(dm(d0, d0), dm(d1, d1));
+      const double R = da(rsq, epssq);
+      const double denom = dm(twopi, R);
+      const double denom2 = dm(kPI, dm(R, R));
+      const double greens = dd(-log(R), fourpi);
+      const double xy = dm(d0, d1);
+      const double d00 = dm(d0, d0), d11 = dm(d1, d1);
+      r[0] = da(r[0], dd(da(dm(-d1, y.rot), dm(d0, y.pot)), denom));
+      r[1] = da(r[1], dd(da(dm(d0, y.rot), dm(d1, y.pot)), denom));
+      r[2] = da(r[2], da(dd(ds(dm(xy, y.rot), dm(d00, y.pot)), denom2), dd(y.pot, denom)));
+      r[3] = da(r[3], ds(dd(ds(dm(d11, y.rot), dm(xy, y.pot)), denom2), dd(y.rot, denom)));
+      r[4] = da(r[4], da(dd(ds(dm(-d00, y.rot), dm(xy, y.pot)), denom2), dd(y.rot, denom)));
+      r[5] = da(r[5], da(dd(ds(dm(-xy, y.rot), dm(d11, y.pot)), denom2), dd(y.pot, denom)));
+      const double e0 = ds(y.x, x0), e1 = ds(y.y, x1);
+      const double pr = dd(__dsqrt_rn(da(dm(e0, e0), dm(e1, e1))), pse_eps);
+      const double p2 = dm(pr, pr);
+      const double p4 = dm(p2, p2);
+      const double pre = ds(da(dm(40.0, ds(1.0, p2)), dm(10.0, p4)), dd(dm(dm(2.0, p2), p4), 3.0));
+      const double lap = dm(pre, dd(exp(-p2), kPI));
+      r[6] = da(r[6], dd(dm(dm(ds(y.s, si), y.area), lap), pse2));
+      r[7] = da(r[7], dm(greens, y.rot));
+      r[8] = da(r[8], dm(greens, y.pot));
+    }
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int k = 0; k < kSweNC; ++k) part[(c * kSweNC + k) * tpad + i] = r[k];
+}
+
+struct SweOut {
+  View u;
+  double *ddot, *du1dx1, *du1dx2, *du2dx1, *du2dx2, *laps, *psi, *phi;
+  int do_velocity;
+};
+
+__global__ void k_swe_out(const double* __restrict__ part, int nchunks, int64_t tpad, int64_t nt,
+                          SweOut o) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  double s[kSweNC];
+#pragma unroll
+  for (int k = 0; k < kSweNC; ++k) s[k] = 0.0;
+  for (int c = 0; c < nchunks; ++c)
+#pragma unroll
+    for (int k = 0; k < kSweNC; ++k) s[k] = da(s[k], part[(int64_t(c) * kSweNC + k) * tpad + i]);
+  if (o.do_velocity) {
+    o.u(i, 0) = s[0];
+    o.u(i, 1) = s[1];
+  }
+  // square(du/dx) + 2 du/dy dv/dx + square(dv/dy)
+  o.ddot[i] = da(da(dm(s[2], s[2]), dm(dm(2.0, s[3]), s[4])), dm(s[5], s[5]));
+  o.du1dx1[i] = s[2];
+  o.du1dx2[i] = s[3];
+  o.du2dx1[i] = s[4];
+  o.du2dx2[i] = s[5];
+  o.laps[i] = s[6];
+  o.psi[i] = s[7];
+  o.phi[i] = s[8];
+}
+
+bool bad_count(int64_t n) { return n < 0 || n > (int64_t(1) << 31) - 1; }
+
+// Targets tx (nt x 2) with surface ts; sources: face slots fx/zeta/sigma/
+// area/mask/sfc (nf); collocated: targets are the face slots themselves.
+void swe_plane_sums(lpm_context& ctx, View tx, const double* ts, int64_t nt, View fx,
+                    const double* zeta, const double* sigma, const double* area,
+                    const uint8_t* mask, const double* sfc, int64_t nf, double eps,
+                    double pse_eps, bool collocated, const SweOut& out) {
+  if (nt == 0) return;
+  ctx.arena.reset();
+  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
+  const int64_t tpad = nb * kSweNT;
+  // chunks: about 4 waves of CTAs
+  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
+  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
+  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
+                    sizeof(SweSrc) * size_t(nf) + sizeof(double) * kSweNC * size_t(nch_max) * tpad +
+                    8 * 4096);
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
+  SweSrc* src = static_cast<SweSrc*>(ctx.arena.take(sizeof(SweSrc) * std::max<int64_t>(ns, 1)));
+  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
+  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
+  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSweNC * size_t(nchunks) * tpad));
+  if (ns > 0) {
+    k_swe_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, sfc,
+                                                                    src2slot, ns, src);
+    ctx.launches++;
+  }
+  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
+  k_swe_plane<<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, eps, pse_eps,
+                                               collocated ? 1 : 0, part, tpad);
+  k_swe_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, nt, out);
+  ctx.launches += 2;
+  LPM_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+}  // namespace lpm
+
+namespace {
+int swe_args(lpm_context* ctx, lpm_view u, double* ddot, double* a, double* b, double* c,
+             double* d, double* laps, double* psi, double* phi, lpm_view x, const double* s,
+             int64_t nt, lpm_view fx, const double* zeta, const double* sigma, const double* area,
+             const uint8_t* mask, const double* fs, int64_t nf, double eps, double pse_eps,
+             int do_velocity) {
+  if (!ctx) return lpm::fail(LPM_ERR_ARG, "null context");
+  if (lpm::bad_count(nt) || lpm::bad_count(nf))
+    return lpm::fail(LPM_ERR_ARG, "count out of range [0, 2^31-1]");
+  if (nt > 0 && (!x.p || !s || !ddot || !a || !b || !c || !d || !laps || !psi || !phi ||
+                 (do_velocity && !u.p)))
+    return lpm::fail(LPM_ERR_ARG, "null target or output array");
+  if (nf > 0 && (!fx.p || !zeta || !sigma || !area || !mask || !fs))
+    return lpm::fail(LPM_ERR_ARG, "null source array");
+  if (!(eps >= 0) || !std::isfinite(eps) || !(pse_eps > 0) || !std::isfinite(pse_eps))
+    return lpm::fail(LPM_ERR_ARG, "eps must be >= 0 and pse_eps > 0, both finite");
+  return LPM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int lpm_swe_plane_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot, double* du1dx1,
+                              double* du1dx2, double* du2dx1, double* du2dx2, double* laps,
+                              double* psi, double* phi, lpm_view vx, const double* vs, int64_t nv,
+                              lpm_view fx, const double* fzeta, const double* fsigma,
+                              const double* farea, const uint8_t* fmask, const double* fs,
+                              int64_t nf, double eps, double pse_eps, int do_velocity) {
+  if (int r = swe_args(ctx, u, ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, vx, vs, nv,
+                       fx, fzeta, fsigma, farea, fmask, fs, nf, eps, pse_eps, do_velocity))
+    return r;
+  try {
+    cudaSetDevice(ctx->device);
+    lpm::SweOut o{lpm::to_view(u), ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, do_velocity};
+    lpm::swe_plane_sums(*ctx, lpm::to_view(vx), vs, nv, lpm::to_view(fx), fzeta, fsigma, farea,
+                        fmask, fs, nf, eps, pse_eps, false, o);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot, double* du1dx1,
+                            double* du1dx2, double* du2dx1, double* du2dx2, double* laps,
+                            double* psi, double* phi, lpm_view fx, const double* fzeta,
+                            const double* fsigma, const double* farea, const uint8_t* fmask,
+                            const double* fs, int64_t nf, double eps, double pse_eps,
+                            int do_velocity) {
+  if (int r = swe_args(ctx, u, ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, fx, fs, nf,
+                       fx, fzeta, fsigma, farea, fmask, fs, nf, eps, pse_eps, do_velocity))
+    return r;
+  try {
+    cudaSetDevice(ctx->device);
+    lpm::SweOut o{lpm::to_view(u), ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, do_velocity};
+    // PlanarSWEFaceSums: collocated = !(eps > 0)
+    lpm::swe_plane_sums(*ctx, lpm::to_view(fx), fs, nf, lpm::to_view(fx), fzeta, fsigma, farea,
+                        fmask, fs, nf, eps, pse_eps, !(eps > 0), o);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+}  // extern "C"

@@ -93,6 +93,37 @@ def sphere_tangency(ctx, udotx, x, u):
     check(lib().lpm_sphere_tangency(ctx.handle, ptr(udotx), view(x), view(u), _n(x)))
 
 
+_SWE_KEYS = ("ddot", "du1dx1", "du1dx2", "du2dx1", "du2dx2", "laps", "psi", "phi")
+
+
+def _swe_outputs(n, like):
+    import torch
+
+    out = {k: torch.zeros(n, dtype=torch.float64, device=like.device) for k in _SWE_KEYS}
+    out["u"] = torch.zeros(n, 2, dtype=torch.float64, device=like.device)
+    return out
+
+
+def swe_plane_vertex_sums(ctx, vx, vs, fx, fzeta, fsigma, farea, fmask, fs, eps, pse_eps,
+                          do_velocity=True):
+    """PlanarSWEVertexSums (src/lpm_swe_kernels.hpp:626-721): dict of outputs."""
+    o = _swe_outputs(_n(vx), vx)
+    check(lib().lpm_swe_plane_vertex_sums(
+        ctx.handle, view(o["u"]), *(ptr(o[k]) for k in _SWE_KEYS), view(vx), ptr(vs), _n(vx),
+        view(fx), ptr(fzeta), ptr(fsigma), ptr(farea), ptr(fmask), ptr(fs), _n(fx), eps, pse_eps,
+        int(do_velocity)))
+    return o
+
+
+def swe_plane_face_sums(ctx, fx, fzeta, fsigma, farea, fmask, fs, eps, pse_eps, do_velocity=True):
+    """PlanarSWEFaceSums (src/lpm_swe_kernels.hpp:787-876): dict of outputs."""
+    o = _swe_outputs(_n(fx), fx)
+    check(lib().lpm_swe_plane_face_sums(
+        ctx.handle, view(o["u"]), *(ptr(o[k]) for k in _SWE_KEYS), view(fx), ptr(fzeta),
+        ptr(fsigma), ptr(farea), ptr(fmask), ptr(fs), _n(fx), eps, pse_eps, int(do_velocity)))
+    return o
+
+
 def ic2d_invariants(ctx, zeta, vel, area, mask):
     import ctypes as C
     out = (C.c_double * 3)()

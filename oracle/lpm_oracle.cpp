@@ -514,4 +514,50 @@ void oracle_err_norms(int ndim, long n, const double* appx,
   out3[2] = lin * safe(lid);
 }
 
+// Planar SWE direct sums with PSE (PlanarSWEVertexSums / PlanarSWEFaceSums,
+// src/lpm_swe_kernels.hpp:626-876; pair term planar_swe_sums_rhs_pse :394-480,
+// reducer rules :559-570; PSE kernel pse::BivariateOrder8::laplacian,
+// src/lpm_pse.hpp:66-72, kernel_input = distance / pse_eps :30-34).
+// out9[9 * i + k]: u, v, du/dx, du/dy, dv/dx, dv/dy, lap(s), psi, phi.
+// collocated: targets are the sources (face sums); then j == i is skipped.
+void oracle_swe_plane_sums(long nt, const double* tx, const double* ts, long ns,
+                           const double* y, const double* zeta, const double* sigma,
+                           const double* area, const unsigned char* mask,
+                           const double* ss, double eps, double pse_eps,
+                           int collocated, double* out9) {
+  const double epssq = eps * eps;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < nt; ++i) {
+    double r[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const double x0 = tx[2 * i], x1 = tx[2 * i + 1];
+    for (long j = 0; j < ns; ++j) {
+      if (mask[j] || (collocated && i == j)) continue;
+      const double d0 = x0 - y[2 * j], d1 = x1 - y[2 * j + 1];
+      const double rsq = d0 * d0 + d1 * d1;
+      const double denom = 2 * PI * (rsq + epssq);
+      const double denom2 = PI * ((rsq + epssq) * (rsq + epssq));
+      const double rot = zeta[j] * area[j];
+      const double pot = sigma[j] * area[j];
+      const double greens = -std::log(rsq + epssq) / (4 * PI);
+      const double xy = d0 * d1;
+      r[0] += (-d1 * rot + d0 * pot) / denom;
+      r[1] += (d0 * rot + d1 * pot) / denom;
+      r[2] += (xy * rot - (d0 * d0) * pot) / denom2 + pot / denom;
+      r[3] += ((d1 * d1) * rot - xy * pot) / denom2 - rot / denom;
+      r[4] += (-(d0 * d0) * rot - xy * pot) / denom2 + rot / denom;
+      r[5] += (-xy * rot - (d1 * d1) * pot) / denom2 + pot / denom;
+      // PSE: r = |y - x| / pse_eps
+      const double e0 = y[2 * j] - x0, e1 = y[2 * j + 1] - x1;
+      const double pr = std::sqrt(e0 * e0 + e1 * e1) / pse_eps;
+      const double prsq = pr * pr;
+      const double lap = (40 * (1 - prsq) + 10 * (prsq * prsq) - 2 * prsq * (prsq * prsq) / 3) *
+                         (std::exp(-prsq) / PI);
+      r[6] += (ss[j] - ts[i]) * area[j] * lap / (pse_eps * pse_eps);
+      r[7] += greens * rot;
+      r[8] += greens * pot;
+    }
+    for (int k = 0; k < 9; ++k) out9[9 * i + k] = r[k];
+  }
+}
+
 }  // extern "C"

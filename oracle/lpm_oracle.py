@@ -34,6 +34,7 @@ def lib() -> C.CDLL:
         vp, l, i, d = C.c_void_p, C.c_long, C.c_int, C.c_double
         sig = {
             "oracle_set_threads": [i],
+            "oracle_swe_plane_sums": [l, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, i, vp],
             "oracle_set_sphere_form": [i],
             "oracle_max_threads": [],
             "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
@@ -182,6 +183,18 @@ class IC2DState:
                                    _p(self.vvel), _p(self.vpsi), self.fx.shape[0], _p(self.fx),
                                    _p(self.fzeta), _p(self.fvel), _p(self.fpsi), _p(self.farea),
                                    _p(self.fmask), float(dt), self.eps, self.cor, self.self_rule)
+
+
+def swe_plane_sums(tx, ts, y, zeta, sigma, area, mask, ss, eps, pse_eps, collocated=False):
+    """Planar SWE sums (n x 9): u, v, du/dx, du/dy, dv/dx, dv/dy, lap(s), psi, phi."""
+    tx, ts, y = _f(tx), _f(ts), _f(y)
+    zeta, sigma, area, ss = _f(zeta), _f(sigma), _f(area), _f(ss)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros((tx.shape[0], 9))
+    lib().oracle_swe_plane_sums(tx.shape[0], _p(tx), _p(ts), y.shape[0], _p(y), _p(zeta),
+                                _p(sigma), _p(area), _p(mask), _p(ss), float(eps),
+                                float(pse_eps), int(collocated), _p(out))
+    return out
 
 
 def invariants(zeta, vel, area, mask):
