@@ -6,8 +6,9 @@
 // its non-empty octants.  Cells are numbered breadth first, so the children
 // of a cell are contiguous; each cell is a contiguous range of the sorted
 // order.  Targets are Morton-sorted the same way and cut into target blocks
-// of 96 to kTargetBlock consecutive targets (padded to kTargetBlock rows),
-// each cut at the coarsest octree boundary of its window.
+// of at most kTargetBlock targets (padded to kTargetBlock rows): the leaves of
+// a target octree, consecutive small sibling leaves packed into one block, so
+// no block straddles a jump of the curve and blocks stay well filled.
 //
 // The reference has no working octree (its LpmOctree/LpmNodeArray sources are
 // not built and lpm_cpu_tree indexes points by loop index); this is the
@@ -130,28 +131,46 @@ TreeTopo build_tree(const double* src_xyz, int64_t nsrc, const double* tgt_xyz, 
     if (t.nchild[i] == 0) t.child0[i] = -1;
     t.max_level = std::max(t.max_level, cells[i].level);
   }
-  // targets: Morton order cut into blocks of 96..kTargetBlock consecutive
-  // targets, each cut placed at the coarsest octree boundary in the window
-  // (the largest key difference), so blocks stay full and do not straddle a
-  // large jump of the curve
+  // targets: Morton order cut into the leaves of an octree with at most
+  // kTargetBlock targets each, so that no block straddles a jump of the curve
   std::vector<uint64_t> tkeys;
   std::vector<int> tperm = ntgt > 0 ? sorted_order(bx, tgt_xyz, ntgt, tkeys) : std::vector<int>{};
   std::vector<std::pair<int, int>> blocks;
-  for (int64_t b0 = 0; b0 < ntgt;) {
-    int64_t cut = std::min<int64_t>(ntgt, b0 + kTargetBlock);
-    if (cut < ntgt) {
-      int best = 65;
-      for (int64_t p = b0 + kTargetBlock * 3 / 4; p <= b0 + kTargetBlock; ++p) {
-        const uint64_t x = tkeys[p - 1] ^ tkeys[p];
-        const int lz = x ? __builtin_clzll(x) : 64;
-        if (lz <= best) {  // coarser (or equal, later) boundary
-          best = lz;
-          cut = p;
-        }
-      }
+  std::vector<C> work;
+  if (ntgt > 0) work.push_back({0, int(ntgt), 0});
+  while (!work.empty()) {
+    const C c = work.back();
+    work.pop_back();
+    if (c.count <= kTargetBlock || c.level >= 21) {  // a leaf, or packed siblings
+      for (int b = 0; b < c.count; b += kTargetBlock)
+        blocks.push_back({c.start + b, std::min(kTargetBlock, c.count - b)});
+      continue;
     }
-    blocks.push_back({int(b0), int(cut - b0)});
-    b0 = cut;
+    const int shift = 3 * (20 - c.level);
+    std::vector<C> kids;
+    int b = c.start;
+    const int e = c.start + c.count;
+    while (b < e) {
+      const uint64_t oct = (tkeys[b] >> shift) & 7;
+      int j = b;
+      while (j < e && ((tkeys[j] >> shift) & 7) == oct) ++j;
+      kids.push_back({b, j - b, c.level + 1});
+      b = j;
+    }
+    // consecutive small siblings share a block (they lie in the same parent
+    // octant); larger ones are split further
+    std::vector<C> split;
+    for (size_t k = 0; k < kids.size();) {
+      if (kids[k].count > kTargetBlock) {
+        split.push_back(kids[k++]);
+        continue;
+      }
+      int s0 = kids[k].start, n0 = 0;
+      while (k < kids.size() && kids[k].count <= kTargetBlock && n0 + kids[k].count <= kTargetBlock)
+        n0 += kids[k++].count;
+      split.push_back({s0, n0, 99});  // level 99: emit as one block
+    }
+    for (auto it = split.rbegin(); it != split.rend(); ++it) work.push_back(*it);
   }
   t.nblocks = int64_t(blocks.size());
   t.tslot.assign(size_t(t.nblocks) * kTargetBlock, -1);
