@@ -809,14 +809,14 @@ def run_c5(args, device):
     advance(hs, st)
     tree_ms, net_ms, nev = ff.timing(False)
     core.lib().lpm_bve_rk4_destroy(hs)
-    tiles = stats["learned_tiles"]
-    flops_tile = 2 * 128 * (48 * 128 + 2 * 128 * 128 + 128 * 16)
+    rows = stats["network_rows"]
+    flops_row = 2 * (48 * 128 + 2 * 128 * 128 + 128 * 16)  # one (target, cell) row, 4 layers
     peaks = {}
     pp = ROOT / "MEASURED_PEAKS.json"
     if pp.exists():
         peaks = json.loads(pp.read_text())
     peak = peaks.get("bf16_tflops")
-    net_tf = tiles * flops_tile / (net_ms / nev * 1e-3) / 1e12 if nev and net_ms > 0 else None
+    net_tf = rows * flops_row / (net_ms / nev * 1e-3) / 1e12 if nev and net_ms > 0 else None
     step_s = ms / args.steps * 1e-3
     return {"metric": METRIC,
             "value": round(4 * ipe / step_s / 1e9, 3), "unit": UNIT, "n_gpus": 1,
@@ -848,7 +848,8 @@ def run_c5(args, device):
                          "peak": peak, "unit": "TFLOP/s",
                          "frac": round(net_tf / peak, 4) if (net_tf and peak) else None,
                          "traffic": None,
-                         "flops_per_tile": flops_tile, "tiles_per_evaluation": tiles,
+                         "flops_per_row": flops_row, "rows_per_evaluation": rows,
+                         "tiles_of_128_rows": -(-rows // 128),
                          "peak_kind": "bf16_tflops of MEASURED_PEAKS.json (burst)"},
             "clocks": clocks, "gpu_launches": launches}
 

@@ -381,8 +381,9 @@ int lpm_farfield_set_weights(lpm_farfield* ff, const float* w,
 int lpm_farfield_grad(lpm_farfield* ff, const float* x, const float* y, int n,
                       float* grad);
 /* Of the last evaluation: far (block, cell) pairs, near (target, source)
- * pairs / 128, learned tiles, blocks on the direct-sum fallback, cells,
- * target blocks.  out: 6 int64.  Synchronous. */
+ * pairs / 128, learned (block, cell) pairs, blocks on the direct-sum
+ * fallback, cells, target blocks, (target, cell) rows the network evaluated.
+ * out: 7 int64.  Synchronous. */
 int lpm_farfield_stats(lpm_farfield* ff, int64_t* out);
 /* Device time of the evaluations since the previous call (tree kernels and
  * network kernel, ms) and their count, then resets; enable != 0 brackets the

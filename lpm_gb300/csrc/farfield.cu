@@ -511,7 +511,12 @@ void lpm_farfield::counts() {
   LPM_CUDA(cudaMemcpyAsync(c.data(), d->cnt, sizeof(int4) * d->nblocks, cudaMemcpyDeviceToHost,
                            ctx->stream));
   LPM_CUDA(cudaStreamSynchronize(ctx->stream));
-  last_far = last_near = last_learn = last_fallback = 0;
+  last_far = last_near = last_learn = last_fallback = last_rows = 0;
+  if (use_net && trained) {
+    unsigned long long r = 0;
+    LPM_CUDA(cudaMemcpy(&r, d->counter + 2, sizeof(r), cudaMemcpyDeviceToHost));
+    last_rows = int64_t(r);
+  }
   std::vector<int4> cells(d->ncells);
   LPM_CUDA(cudaMemcpy(cells.data(), d->cells, sizeof(int4) * d->ncells, cudaMemcpyDeviceToHost));
   std::vector<int> nearl(size_t(d->nblocks) * kNearCap);

@@ -77,7 +77,7 @@ struct lpm_farfield {
   // network (host copy of the FP32 master weights and input normalisation)
   std::vector<float> w;       // kNParam
   std::vector<float> norm;    // mu[48], isd[48], out_scale
-  int64_t last_far = 0, last_near = 0, last_learn = 0, last_fallback = 0;
+  int64_t last_far = 0, last_near = 0, last_learn = 0, last_fallback = 0, last_rows = 0;
   // optional CUDA-event timing of evaluations (not inside graph capture)
   bool timing = false;
   std::vector<void*> events;  // cudaEvent_t triples: start, tree done, network done

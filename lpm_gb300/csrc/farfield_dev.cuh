@@ -24,7 +24,7 @@ struct FFDevice {
   float4* box = nullptr;  // target block centre and radius
   int *far = nullptr, *near = nullptr, *lrn = nullptr;  // per-block lists
   int4* cnt = nullptr;    // (far, near, learned, overflow) per block
-  int* counter = nullptr; // work counter of the persistent network kernel
+  int* counter = nullptr; // [0] work counter of the network kernel, [2..3] rows (u64)
   std::vector<void*> allocs;
   ~FFDevice();
   void* alloc(size_t bytes);

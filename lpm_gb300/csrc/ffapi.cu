@@ -219,6 +219,7 @@ int lpm_farfield_stats(lpm_farfield* ff, int64_t* out) {
     out[3] = ff->last_fallback;
     out[4] = ff->d->ncells;
     out[5] = ff->d->nblocks;
+    out[6] = ff->last_rows;
     return LPM_OK;
   } catch (...) {
     return lpm::handle_exception();

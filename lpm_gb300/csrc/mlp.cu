@@ -61,10 +61,16 @@ constexpr int kSmDY = kSmA3 + 128 * kHid * 2;
 constexpr int kSmTrain = kSmDY + 128 * kOut * 2;  // 196608
 // inference: kInfWG independent warpgroups, each with an activation tile H
 // (its input tile X aliases the start of H: layer 1 reads X before its
-// epilogue writes H) and a cell record
+// epilogue writes H; after the output layer H holds the rows' corrections),
+// the block's target positions and a buffer of pending (target, cell) rows
 constexpr int kInfWG = 4;
-constexpr int kInfWGBytes = 128 * kHid * 2 + 512;
-constexpr int kSmInfer = kSmWEnd + kInfWG * kInfWGBytes;  // 215040
+constexpr int kRowCap = 256;
+constexpr int kInfH = 128 * kHid * 2;
+constexpr int kInfX = kInfH;                       // float4 x 128 targets
+constexpr int kInfRows = kInfX + 128 * 16;         // uint32 (target | cell << 8) x kRowCap
+constexpr int kInfCnt = kInfRows + kRowCap * 4;    // per-warp counts
+constexpr int kInfWGBytes = kInfCnt + 64;
+constexpr int kSmInfer = kSmWEnd + kInfWG * kInfWGBytes;
 
 // element offsets of the matrices in the BF16 weight image and the FP32
 // master vector (same order)
@@ -224,13 +230,17 @@ struct MlpArgs {
   int64_t wstride;
   float eps, rho_min;
   int* counter;
+  unsigned long long* rows;  // (target, cell) rows evaluated
   int* err;
 };
 
 // Persistent, one CTA (512 threads) per SM: four independent warpgroups, each
 // with its own quarter of TMEM (128 columns), mbarrier, named barrier and
-// activation tile, pull target blocks; per block, one tile per learned cell,
-// the correction accumulated per target in registers.  While one warpgroup
+// activation tile, pull target blocks.  Per block, a warpgroup walks the
+// learned cells and appends the (target, cell) pairs that need the
+// correction (rho >= rho_min) to a row buffer, cell-major; every 128 rows
+// make one dense tile.  After a tile each thread adds, in row order, the
+// rows that belong to its own target (deterministic).  While one warpgroup
 // runs its SiLU epilogue the others keep the tensor core busy.
 __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -238,7 +248,7 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   __shared__ uint32_t tslot;
   __shared__ int blk[kInfWG];
   __shared__ float nrm[2 * kIn + 1];
-  const int t = threadIdx.x, w = t >> 5, g = t >> 7, lt = t & 127;
+  const int t = threadIdx.x, w = t >> 5, g = t >> 7, lt = t & 127, lane = t & 31;
   load_weights(sm, a.wbf);
   for (int i = t; i < 2 * kIn + 1; i += blockDim.x) nrm[i] = a.norm[i];
   if (t == 0) {
@@ -252,10 +262,14 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   const uint32_t tb = tslot + 128u * g;
   const WgSync s{1u + unsigned(g)};
   const int ho = kSmWEnd + g * kInfWGBytes;  // H, with X at its start
-  float* cell = reinterpret_cast<float*>(sm + ho + 128 * kHid * 2);
+  float4* xs = reinterpret_cast<float4*>(sm + ho + kInfX);
+  uint32_t* rows = reinterpret_cast<uint32_t*>(sm + ho + kInfRows);
+  int* wcnt = reinterpret_cast<int*>(sm + ho + kInfCnt);
+  float4* contrib = reinterpret_cast<float4*>(sm + ho);  // over H after the output layer
   uint32_t ph = 0;
   bool ok = true;
   const float oscale = nrm[2 * kIn];
+  const float rho_min = a.rho_min;
   for (;;) {
     s.sync();
     if (lt == 0) blk[g] = atomicAdd(a.counter, 1);
@@ -264,39 +278,84 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
     if (b >= a.nblocks) break;
     const int4 nc = a.cnt[b];
     if (nc.w || nc.z == 0) continue;
-    const float4 x = a.xt[b * kTargetBlock + lt];
+    const float4 xme = a.xt[b * kTargetBlock + lt];
+    xs[lt] = xme;
     float acc[3] = {0.f, 0.f, 0.f};
-    for (int k = 0; k < nc.z && ok; ++k) {
-      const int c = a.lrn[b * kLearnCap + k];
-      s.sync();
-      if (lt < kCellF / 4)
-        reinterpret_cast<float4*>(cell)[lt] = reinterpret_cast<const float4*>(a.cd + int64_t(c) * kCellF)[lt];
-      s.sync();
-      float d[3];
-      ff::to_cell(cell, x.x, x.y, x.z, d);
-      const ff::PairGeo pg = ff::pair_geo(cell, d);
-      const bool use = x.w > 0.f && pg.rho >= a.rho_min && pg.rho <= 1.f;
+    int nrows = 0;  // rows pending in the buffer (same value in every thread)
+    int total = 0;  // rows of this block
+    // One dense tile of the first m rows (m <= 128; rows >= m are padding).
+    auto run_tile = [&](int m) -> bool {
+      const bool have = lt < m;
+      const uint32_t code = have ? rows[lt] : 0u;
+      const int rt = int(code & 0xffu), rc = int(code >> 8);
+      const float* cell = a.cd + int64_t(rc) * kCellF;
+      const float4 x = xs[rt];
       float f[kIn];
-      ff::pair_features(cell, pg, a.eps, f);
+      ff::PairGeo pg;
+      {
+        float d[3];
+        ff::to_cell(cell, x.x, x.y, x.z, d);
+        pg = ff::pair_geo(cell, d);
+        ff::pair_features(cell, pg, a.eps, f);
+      }
       f[kBiasIn] = 1.f;
 #pragma unroll
       for (int i = kBiasIn + 1; i < kIn; ++i) f[i] = 0.f;
 #pragma unroll
-      for (int i = 0; i < kIn; ++i) f[i] = (f[i] - nrm[i]) * nrm[kIn + i];
+      for (int i = 0; i < kIn; ++i) f[i] = have ? (f[i] - nrm[i]) * nrm[kIn + i] : 0.f;
       write_x_row(sm + ho, lt, f);
-      ok = forward(sm, tb, &bar[g], ph, s, ho, ho, ho, ho);
-      if (!ok) break;
+      if (!forward(sm, tb, &bar[g], ph, s, ho, ho, ho, ho)) return false;
       float o[16];
       tc::ld16(tc::lane_addr(tb, w, 0), o);
-      if (use) {
-        float dw[3];
-        ff::correction(cell, pg, o, oscale, x.x, x.y, x.z, dw);
-        acc[0] += dw[0];
-        acc[1] += dw[1];
-        acc[2] += dw[2];
+      float dw[3] = {0.f, 0.f, 0.f};
+      if (have) ff::correction(cell, pg, o, oscale, x.x, x.y, x.z, dw);
+      tc::fence_before();
+      s.sync();  // the output layer has read H: reuse it for the corrections
+      contrib[lt] = make_float4(dw[0], dw[1], dw[2], __int_as_float(have ? rt : -1));
+      s.sync();
+      for (int r = 0; r < m; ++r) {
+        const float4 cr = contrib[r];
+        if (__float_as_int(cr.w) == lt) {
+          acc[0] += cr.x;
+          acc[1] += cr.y;
+          acc[2] += cr.z;
+        }
+      }
+      s.sync();
+      return true;
+    };
+    for (int k = 0; k < nc.z && ok; ++k) {
+      const int c = a.lrn[b * kLearnCap + k];
+      const float* cell = a.cd + int64_t(c) * kCellF;
+      const float e0 = xme.x - cell[0], e1 = xme.y - cell[1], e2 = xme.z - cell[2];
+      const float D2 = e0 * e0 + e1 * e1 + e2 * e2;
+      const float h = cell[4];
+      const bool v = xme.w > 0.f && h * h >= rho_min * rho_min * D2 && h * h <= D2;
+      const unsigned bal = __ballot_sync(0xffffffffu, v);
+      if (lane == 0) wcnt[w & 3] = __popc(bal);
+      s.sync();
+      int base = nrows;
+      for (int q = 0; q < (w & 3); ++q) base += wcnt[q];
+      const int added = wcnt[0] + wcnt[1] + wcnt[2] + wcnt[3];
+      if (v) rows[base + __popc(bal & ((1u << lane) - 1u))] = uint32_t(lt) | (uint32_t(c) << 8);
+      nrows += added;
+      total += added;
+      s.sync();
+      if (nrows >= 128) {
+        ok = run_tile(128);
+        if (!ok) break;
+        // move the remaining rows to the front
+        const int rest = nrows - 128;
+        const uint32_t mv = lt < rest ? rows[128 + lt] : 0u;
+        s.sync();
+        if (lt < rest) rows[lt] = mv;
+        nrows = rest;
+        s.sync();
       }
     }
+    if (ok && nrows > 0) ok = run_tile(nrows);
     if (!ok) break;
+    if (lt == 0) atomicAdd(a.rows, static_cast<unsigned long long>(total));
     const int64_t tt = a.tslot[b * kTargetBlock + lt];
     if (tt >= 0) {
       a.wout[tt] += acc[0];
@@ -731,7 +790,7 @@ void ff_prepare_kernels() {
 
 void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int64_t wstride,
                    double eps, double rho_min) {
-  LPM_CUDA(cudaMemsetAsync(d.counter, 0, sizeof(int), ctx.stream));
+  LPM_CUDA(cudaMemsetAsync(d.counter, 0, 4 * sizeof(int), ctx.stream));
   MlpArgs a;
   a.xt = d.xt;
   a.tslot = d.tslot;
@@ -746,6 +805,7 @@ void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int6
   a.eps = float(eps);
   a.rho_min = float(rho_min);
   a.counter = d.counter;
+  a.rows = reinterpret_cast<unsigned long long*>(d.counter + 2);
   a.err = ctx.d_err;
   const int grid = int(std::min<int64_t>(d.nblocks, ctx.num_sms));
   k_ff_mlp<<<grid, 128 * kInfWG, kSmInfer, ctx.stream>>>(a);

@@ -78,10 +78,11 @@ class FarField:
         return g
 
     def stats(self) -> dict:
-        out = (C.c_int64 * 6)()
+        out = (C.c_int64 * 7)()
         check(lib().lpm_farfield_stats(self._h, out))
-        return {"far_pairs": out[0], "near_pairs_x128": out[1], "learned_tiles": out[2],
-                "fallback_blocks": out[3], "cells": out[4], "target_blocks": out[5]}
+        return {"far_pairs": out[0], "near_pairs_x128": out[1], "learned_pairs": out[2],
+                "fallback_blocks": out[3], "cells": out[4], "target_blocks": out[5],
+                "network_rows": out[6]}
 
     def timing(self, enable: bool) -> tuple[float, float, int]:
         """(tree ms, network ms, evaluations) since the last call; then
