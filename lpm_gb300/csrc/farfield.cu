@@ -99,10 +99,12 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
     for (int k = 0; k < 5; ++k) a[k] += f[k];
   }
   block_sum128<5>(a, sh);
-  const double c[3] = {a[0] / n, a[1] / n, a[2] / n};
-  const double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-  double q[9];
-  {
+  // centre and frame: one thread (FP64 is 1/64 of FP32 on this part), shared
+  __shared__ float geo[16];
+  __shared__ double cnorm;
+  if (t == 0) {
+    const double c[3] = {a[0] / n, a[1] / n, a[2] / n};
+    const double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
     double nn[3] = {1, 0, 0};
     if (cn > 0) nn[0] = c[0] / cn, nn[1] = c[1] / cn, nn[2] = c[2] / cn;
     const double r[3] = {fabs(nn[2]) < 0.9 ? 0.0 : 1.0, 0.0, fabs(nn[2]) < 0.9 ? 1.0 : 0.0};
@@ -111,11 +113,19 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
     e1[0] /= l, e1[1] /= l, e1[2] /= l;
     const double e2[3] = {nn[1] * e1[2] - nn[2] * e1[1], nn[2] * e1[0] - nn[0] * e1[2],
                           nn[0] * e1[1] - nn[1] * e1[0]};
-    for (int k = 0; k < 3; ++k) q[k] = e1[k], q[3 + k] = e2[k], q[6 + k] = nn[k];
+    for (int k = 0; k < 3; ++k) {
+      geo[k] = float(c[k]);
+      geo[3 + k] = float(e1[k]);
+      geo[6 + k] = float(e2[k]);
+      geo[9 + k] = float(nn[k]);
+    }
+    cnorm = cn;
   }
-  const float cf[3] = {float(c[0]), float(c[1]), float(c[2])};
+  __syncthreads();
+  const float cf[3] = {geo[0], geo[1], geo[2]};
   float qf[9];
-  for (int k = 0; k < 9; ++k) qf[k] = float(q[k]);
+  for (int k = 0; k < 9; ++k) qf[k] = geo[3 + k];
+  const double cn = cnorm;
   // pass 2: moments about the (FP32) centre in the cell frame
   double M[35];
 #pragma unroll
