@@ -75,6 +75,7 @@ __device__ double block_max128(double x, double* sh) {
 // One CTA (128 threads) per cell.
 __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
                                                   const int4* __restrict__ cells, int ncells,
+                                                  float theta, float rmax,
                                                   float* __restrict__ cd) {
   __shared__ double sh[5 * 40];
   const int cell = blockIdx.x;
@@ -126,12 +127,28 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
   float qf[9];
   for (int k = 0; k < 9; ++k) qf[k] = geo[3 + k];
   const double cn = cnorm;
-  // pass 2: moments about the (FP32) centre in the cell frame
+  // pass 2: radius about the (FP32) centre
+  float hmax = 0.f;
+  for (int i = t; i < n; i += 128) {
+    const float4 p = ys[s0 + i];
+    const float x0 = p.x - cf[0], x1 = p.y - cf[1], x2 = p.z - cf[2];
+    hmax = fmaxf(hmax, x0 * x0 + x1 * x1 + x2 * x2);
+  }
+  __shared__ double hsh;
+  {
+    const double hm = block_max128(double(hmax), sh);
+    if (t == 0) hsh = sqrt(hm);
+    __syncthreads();
+  }
+  const double h = hsh;
+  // no target (all within rmax of the origin) can accept a cell whose radius
+  // exceeds theta * (|c| + rmax): its moments are never used
+  const bool skip = h > double(theta) * (cn + double(rmax));
+  // pass 3: moments in the cell frame
   double M[35];
 #pragma unroll
   for (int k = 0; k < 35; ++k) M[k] = 0.0;
-  float hmax = 0.f;
-  for (int b0 = 0; b0 < n; b0 += 128 * 32) {
+  for (int b0 = 0; b0 < (skip ? 0 : n); b0 += 128 * 32) {
     float m[35];
 #pragma unroll
     for (int k = 0; k < 35; ++k) m[k] = 0.f;
@@ -142,7 +159,6 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
       const float d0 = qf[0] * x0 + qf[1] * x1 + qf[2] * x2;
       const float d1 = qf[3] * x0 + qf[4] * x1 + qf[5] * x2;
       const float d2 = qf[6] * x0 + qf[7] * x1 + qf[8] * x2;
-      hmax = fmaxf(hmax, d0 * d0 + d1 * d1 + d2 * d2);
       float p0[5], p1[5], p2[5];
       p0[0] = p1[0] = p2[0] = 1.f;
 #pragma unroll
@@ -156,7 +172,6 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
     for (int k = 0; k < 35; ++k) M[k] += m[k];
   }
   block_sum128<35>(M, sh);
-  const double h = sqrt(block_max128(double(hmax), sh));
   // record: every thread holds the reduced moments; the fields are written
   // by different threads
   float* r = cd + int64_t(cell) * kCellF;
@@ -299,7 +314,7 @@ __global__ void __launch_bounds__(128) k_ff_eval(
     const int4* __restrict__ cnt, float c0, double* __restrict__ wout, int64_t wstride) {
   __shared__ float4 buf[kNearBuf];
   __shared__ float cell[kFarBatch][kCellF];
-  __shared__ int ofs[9];
+  __shared__ int4 lf[8];
   const int64_t b = blockIdx.x;
   const int t = threadIdx.x;
   const float4 x = xt[b * kTargetBlock + t];
@@ -319,35 +334,30 @@ __global__ void __launch_bounds__(128) k_ff_eval(
       two_sum_acc(S2, C2, w2);
     }
   } else {
-    // near leaves, up to 8 per batch (<= 512 sources)
+    // near leaves, up to 8 per batch (<= 512 sources); the 8 leaf records are
+    // loaded by 8 threads at once
     const int* N = near + b * kNearCap;
     for (int l0 = 0; l0 < nc.y; l0 += 8) {
       const int nl = min(8, nc.y - l0);
       __syncthreads();
-      if (t == 0) {
-        int o = 0;
-        for (int k = 0; k < nl; ++k) {
-          ofs[k] = o;
-          o += min(cells[N[l0 + k]].y, kMaxLeaf);
-        }
-        ofs[nl] = o;
-      }
+      if (t < nl) lf[t] = cells[N[l0 + t]];
       __syncthreads();
+      int o = 0;
       for (int k = 0; k < nl; ++k) {
-        const int4 ci = cells[N[l0 + k]];
-        const int m = ofs[k + 1] - ofs[k];
-        for (int i = t; i < m; i += 128) buf[ofs[k] + i] = ys[ci.x + i];
+        const int4 ci = lf[k];
+        const int m = min(ci.y, kMaxLeaf);
+        for (int i = t; i < m; i += 128) buf[o + i] = ys[ci.x + i];
+        o += m;
       }
       __syncthreads();
       float w0 = 0.f, w1 = 0.f, w2 = 0.f;
-      const int m = ofs[nl];
-      for (int i = 0; i < m; ++i) chord_acc(x.x, x.y, x.z, buf[i], c0, w0, w1, w2);
+      for (int i = 0; i < o; ++i) chord_acc(x.x, x.y, x.z, buf[i], c0, w0, w1, w2);
       two_sum_acc(S0, C0, w0);
       two_sum_acc(S1, C1, w1);
       two_sum_acc(S2, C2, w2);
       // leaves larger than kMaxLeaf (coincident points at the deepest level)
       for (int k = 0; k < nl; ++k) {
-        const int4 ci = cells[N[l0 + k]];
+        const int4 ci = lf[k];
         if (ci.y <= kMaxLeaf) continue;
         float v0 = 0.f, v1 = 0.f, v2 = 0.f;
         for (int i = kMaxLeaf; i < ci.y; ++i) chord_acc(x.x, x.y, x.z, ys[ci.x + i], c0, v0, v1, v2);
@@ -402,7 +412,7 @@ void* FFDevice::alloc(size_t bytes) {
 }
 
 void ff_cells(lpm_context& ctx, const float4* ys, const int4* cells, int ncells, float* cd) {
-  k_ff_cells<<<ncells, 128, 0, ctx.stream>>>(ys, cells, ncells, cd);
+  k_ff_cells<<<ncells, 128, 0, ctx.stream>>>(ys, cells, ncells, 1.0f, 1e30f, cd);
   ctx.launches++;
   LPM_CUDA(cudaGetLastError());
 }
@@ -412,7 +422,7 @@ void ff_launch_tree(lpm_context& ctx, FFDevice& d, const void* tgt, const void* 
   cudaStream_t st = ctx.stream;
   k_ff_sort_src<<<unsigned((d.nsrc + 255) / 256), 256, 0, st>>>(static_cast<const double4*>(src),
                                                                  d.perm, d.nsrc, d.ys);
-  k_ff_cells<<<d.ncells, 128, 0, st>>>(d.ys, d.cells, d.ncells, d.cd);
+  k_ff_cells<<<d.ncells, 128, 0, st>>>(d.ys, d.cells, d.ncells, float(theta), d.rmax, d.cd);
   k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4*>(tgt), d.tslot,
                                                     d.xt, d.box);
   k_ff_lists<<<unsigned((d.nblocks + 63) / 64), 64, 0, st>>>(d.cd, d.cells, d.box, d.nblocks,
@@ -447,6 +457,12 @@ void lpm_farfield::build(const double* src_xyz, int64_t nsrc, const double* tgt_
     nd->ntgt = ntgt;
     nd->ncells = int(tp.start.size());
     nd->nblocks = tp.nblocks;
+    double r2 = 0;
+    for (int64_t i = 0; i < ntgt; ++i)
+      r2 = std::max(r2, tgt_xyz[3 * i] * tgt_xyz[3 * i] + tgt_xyz[3 * i + 1] * tgt_xyz[3 * i + 1] +
+                            tgt_xyz[3 * i + 2] * tgt_xyz[3 * i + 2]);
+    // targets move between tree builds: keep a generous margin
+    nd->rmax = float(1.1 * std::sqrt(r2) + 0.1);
     nd->perm = static_cast<int*>(nd->alloc(sizeof(int) * nsrc));
     nd->tslot = static_cast<int*>(nd->alloc(sizeof(int) * kTargetBlock * size_t(std::max<int64_t>(nd->nblocks, 1))));
     nd->cells = static_cast<int4*>(nd->alloc(sizeof(int4) * nd->ncells));

@@ -15,6 +15,7 @@ namespace lpm {
 struct FFDevice {
   int64_t nsrc = 0, ntgt = 0, nblocks = 0;
   int ncells = 0;
+  float rmax = 1e30f;  // bound on |target| (with margin) at the last tree build
   int* perm = nullptr;    // sorted source -> packed source index
   int* tslot = nullptr;   // block * 128 + row -> packed target index or -1
   int4* cells = nullptr;  // (start, count, first child, child count)
