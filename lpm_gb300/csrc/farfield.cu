@@ -42,13 +42,14 @@ __global__ void k_ff_sort_src(const double4* __restrict__ src, const int* __rest
   ys[k] = make_float4(float(s.x), float(s.y), float(s.z), float(s.w));
 }
 
-// Fixed-order block reduction of nv doubles held by each of 128 threads.
-template <int NV>
-__device__ void block_sum128(double* v, double* sh) {
+// Fixed-order block reduction of NV values held by each of 128 threads (the
+// result in every thread).
+template <int NV, class T>
+__device__ void block_sum128(T* v, T* sh) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
 #pragma unroll
   for (int i = 0; i < NV; ++i) {
-    double x = v[i];
+    T x = v[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) sh[w * NV + i] = x;
@@ -61,13 +62,14 @@ __device__ void block_sum128(double* v, double* sh) {
   __syncthreads();
 }
 
-__device__ double block_max128(double x, double* sh) {
+template <class T>
+__device__ T block_max128(T x, T* sh) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+  for (int o = 16; o > 0; o >>= 1) x = max(x, __shfl_down_sync(0xffffffffu, x, o));
   if (lane == 0) sh[w] = x;
   __syncthreads();
-  x = fmax(fmax(sh[0], sh[1]), fmax(sh[2], sh[3]));
+  x = max(max(sh[0], sh[1]), max(sh[2], sh[3]));
   __syncthreads();
   return x;
 }
@@ -77,27 +79,23 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
                                                   const int4* __restrict__ cells, int ncells,
                                                   float theta, float rmax,
                                                   float* __restrict__ cd) {
-  __shared__ double sh[5 * 40];
+  // FP32 throughout the per-point passes and reductions (the FP64 pipe is
+  // 1/64 of FP32 on this part; the expansion is evaluated in FP32 anyway)
+  __shared__ float sh[5 * 40];
+  __shared__ float msh[35];
   const int cell = blockIdx.x;
   if (cell >= ncells) return;
   const int4 ci = cells[cell];
   const int s0 = ci.x, n = ci.y, t = threadIdx.x;
-  // pass 1: centre, S, sum g (FP32 per 32-point batch per thread, FP64 across
-  // batches: the FP64 pipe is 1/64 of FP32 on this part)
-  double a[5] = {0, 0, 0, 0, 0};
-  for (int b0 = 0; b0 < n; b0 += 128 * 32) {
-    float f[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    const int e = min(n, b0 + 128 * 32);
-    for (int i = b0 + t; i < e; i += 128) {
-      const float4 p = ys[s0 + i];
-      f[0] += p.x;
-      f[1] += p.y;
-      f[2] += p.z;
-      f[3] += fabsf(p.w);
-      f[4] += p.w;
-    }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) a[k] += f[k];
+  // pass 1: centre, S, sum g
+  float a[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = t; i < n; i += 128) {
+    const float4 p = ys[s0 + i];
+    a[0] += p.x;
+    a[1] += p.y;
+    a[2] += p.z;
+    a[3] += fabsf(p.w);
+    a[4] += p.w;
   }
   block_sum128<5>(a, sh);
   // centre and frame: one thread (FP64 is 1/64 of FP32 on this part), shared
@@ -134,26 +132,16 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
     const float x0 = p.x - cf[0], x1 = p.y - cf[1], x2 = p.z - cf[2];
     hmax = fmaxf(hmax, x0 * x0 + x1 * x1 + x2 * x2);
   }
-  __shared__ double hsh;
-  {
-    const double hm = block_max128(double(hmax), sh);
-    if (t == 0) hsh = sqrt(hm);
-    __syncthreads();
-  }
-  const double h = hsh;
+  const double h = sqrt(double(block_max128(hmax, sh)));
   // no target (all within rmax of the origin) can accept a cell whose radius
   // exceeds theta * (|c| + rmax): its moments are never used
   const bool skip = h > double(theta) * (cn + double(rmax));
   // pass 3: moments in the cell frame
-  double M[35];
+  float m[35];
 #pragma unroll
-  for (int k = 0; k < 35; ++k) M[k] = 0.0;
-  for (int b0 = 0; b0 < (skip ? 0 : n); b0 += 128 * 32) {
-    float m[35];
-#pragma unroll
-    for (int k = 0; k < 35; ++k) m[k] = 0.f;
-    const int e = min(n, b0 + 128 * 32);
-    for (int i = b0 + t; i < e; i += 128) {
+  for (int k = 0; k < 35; ++k) m[k] = 0.f;
+  {
+    for (int i = skip ? n : t; i < n; i += 128) {
       const float4 p = ys[s0 + i];
       const float x0 = p.x - cf[0], x1 = p.y - cf[1], x2 = p.z - cf[2];
       const float d0 = qf[0] * x0 + qf[1] * x1 + qf[2] * x2;
@@ -168,10 +156,11 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
         m[k] = fmaf(p.w, p0[ff::mono_exp(k, 0)] * p1[ff::mono_exp(k, 1)] * p2[ff::mono_exp(k, 2)], m[k]);
       });
     }
-#pragma unroll
-    for (int k = 0; k < 35; ++k) M[k] += m[k];
   }
-  block_sum128<35>(M, sh);
+  block_sum128<35>(m, sh);
+  if (t < 35) msh[t] = m[t];
+  __syncthreads();
+  const float* M = msh;
   // record: every thread holds the reduced moments; the fields are written
   // by different threads
   float* r = cd + int64_t(cell) * kCellF;
