@@ -867,7 +867,7 @@ def main():
                          "c5: level 8 on the learned octree far field")
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
-    ap.add_argument("--ff-rho-min", type=float, default=0.2,
+    ap.add_argument("--ff-rho-min", type=float, default=0.25,
                     help="c5: learned correction for cells with h/(D - r_block) >= this")
     ap.add_argument("--ff-save", default=None, help="c5: save the trained network (.npz)")
     ap.add_argument("--ff-weights", default=None,

@@ -105,7 +105,7 @@ class BVERK4 {
 // Octree far field with the learned correction (no reference counterpart).
 class FarField {
  public:
-  explicit FarField(Context& c, double theta = 0.5, int leaf_max = 64, double rho_min = 0.15) {
+  explicit FarField(Context& c, double theta = 0.5, int leaf_max = 64, double rho_min = 0.25) {
     require(lpm_farfield_create(c.get(), &h_, theta, leaf_max, rho_min), "FarField");
   }
   ~FarField() { lpm_farfield_destroy(h_); }

@@ -68,7 +68,7 @@ struct TrainCfg {
 
 struct lpm_farfield {
   lpm_context* ctx = nullptr;
-  double theta = 0.5, rho_min = 0.15;
+  double theta = 0.5, rho_min = 0.25;
   int leaf_max = 64;
   bool use_net = false;
   bool trained = false;

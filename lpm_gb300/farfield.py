@@ -23,7 +23,7 @@ NIN = 48
 
 
 class FarField:
-    def __init__(self, theta: float = 0.5, leaf_max: int = 64, rho_min: float = 0.15,
+    def __init__(self, theta: float = 0.5, leaf_max: int = 64, rho_min: float = 0.25,
                  ctx=None, device: int = 0):
         self.ctx = ctx if ctx is not None else default_context(device)
         self.theta, self.leaf_max, self.rho_min = float(theta), int(leaf_max), float(rho_min)
