@@ -283,6 +283,12 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
     float acc[3] = {0.f, 0.f, 0.f};
     int nrows = 0;  // rows pending in the buffer (same value in every thread)
     int total = 0;  // rows of this block
+    // this thread's pending rows (at most one per cell, increasing); past 8
+    // it falls back to scanning every row of a tile -- same order, same sum
+    constexpr int kMine = 8;
+    int mine[kMine];
+    int nmine = 0;
+    bool scan_all = false;
     // One dense tile of the first m rows (m <= 128; rows >= m are padding).
     auto run_tile = [&](int m) -> bool {
       const bool have = lt < m;
@@ -313,13 +319,41 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
       s.sync();  // the output layer has read H: reuse it for the corrections
       contrib[lt] = make_float4(dw[0], dw[1], dw[2], __int_as_float(have ? rt : -1));
       s.sync();
-      for (int r = 0; r < m; ++r) {
-        const float4 cr = contrib[r];
-        if (__float_as_int(cr.w) == lt) {
-          acc[0] += cr.x;
-          acc[1] += cr.y;
-          acc[2] += cr.z;
+      if (scan_all) {
+        for (int r = 0; r < m; ++r) {
+          const float4 cr = contrib[r];
+          if (__float_as_int(cr.w) == lt) {
+            acc[0] += cr.x;
+            acc[1] += cr.y;
+            acc[2] += cr.z;
+          }
         }
+      } else {
+        int keep = 0;
+#pragma unroll
+        for (int i = 0; i < kMine; ++i) {
+          if (i < nmine) {
+            if (mine[i] < m) {
+              const float4 cr = contrib[mine[i]];
+              acc[0] += cr.x;
+              acc[1] += cr.y;
+              acc[2] += cr.z;
+            } else {
+              ++keep;
+            }
+          }
+        }
+        // drop the consumed rows (they are the first ones), renumber the rest
+#pragma unroll
+        for (int i = 0; i < kMine; ++i) {
+          const int src = i + (nmine - keep);
+          int v = 0;
+#pragma unroll
+          for (int q = 0; q < kMine; ++q)
+            if (q == src) v = mine[q];
+          if (i < keep) mine[i] = v - m;
+        }
+        nmine = keep;
       }
       s.sync();
       return true;
@@ -337,7 +371,18 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
       int base = nrows;
       for (int q = 0; q < (w & 3); ++q) base += wcnt[q];
       const int added = wcnt[0] + wcnt[1] + wcnt[2] + wcnt[3];
-      if (v) rows[base + __popc(bal & ((1u << lane) - 1u))] = uint32_t(lt) | (uint32_t(c) << 8);
+      if (v) {
+        const int pos = base + __popc(bal & ((1u << lane) - 1u));
+        rows[pos] = uint32_t(lt) | (uint32_t(c) << 8);
+        if (nmine < kMine) {
+#pragma unroll
+          for (int q = 0; q < kMine; ++q)
+            if (q == nmine) mine[q] = pos;
+          ++nmine;
+        } else {
+          scan_all = true;
+        }
+      }
       nrows += added;
       total += added;
       s.sync();

@@ -223,3 +223,71 @@ def test_argument_errors(gpu_ctx):
         ff.set_network(True)  # nothing trained or loaded
     with pytest.raises(LpmError):
         ff.stats()  # no evaluation yet
+
+
+def test_farfield_deterministic_and_strided_views(gpu_ctx):
+    """Two evaluations with the network give bitwise equal results; targets
+    and outputs in a component-major (Kokkos LayoutLeft) layout give the same
+    velocities as row-major ones."""
+    import torch
+
+    from lpm_gb300.farfield import FarField
+
+    vx, fx, fa, fm, fz = _mesh(5)
+    eps = 0.01
+    ff = FarField(ctx=gpu_ctx)
+    ff.set_weights(_rand_net(7) * 0.1,
+                   np.concatenate([np.zeros(48), np.ones(48), [1e-3]]).astype(np.float32))
+    ff.set_network(True)
+    u1 = _ff_velocity(ff, vx, fx, fz, fa, fm, eps)
+    u2 = _ff_velocity(ff, vx, fx, fz, fa, fm, eps)
+    assert np.array_equal(u1, u2)
+    assert ff.stats()["network_rows"] > 0
+    d = torch.device("cuda", gpu_ctx.device)
+    xl = torch.tensor(np.ascontiguousarray(vx.T), device=d).t()   # strides (1, n)
+    ul = torch.zeros(3, vx.shape[0], dtype=torch.float64, device=d).t()
+    fxl = torch.tensor(np.ascontiguousarray(fx.T), device=d).t()
+    ff.velocity(ul, xl, fxl, torch.tensor(fz, device=d), torch.tensor(fa, device=d),
+                torch.tensor(fm, device=d), eps)
+    torch.cuda.synchronize()
+    assert np.array_equal(ul.cpu().numpy(), u1)
+
+
+def test_rk4_farfield_rebuilds_tree(gpu_ctx):
+    """A stepper that rebuilds its tree every step stays within the far
+    field's error of one that keeps the first tree."""
+    import ctypes as C
+
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.farfield import FarField
+
+    eps, dt = 0.01, 0.005
+    vx, fx, fa, fm, fz = _mesh(4)
+    vz = core.eval_ic(core.IC_RH54, (2 * math.pi / 12.5, -2 * math.pi / 12.5), vx)
+    d = torch.device("cuda", gpu_ctx.device)
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+    out, keep = [], []
+    for every in (0, 1):
+        t = {k: torch.tensor(v, device=d) for k, v in
+             dict(vx=vx, fx=fx, fa=fa, fm=fm, fz=fz, vz=vz).items()}
+        vu, fu = torch.zeros_like(t["vx"]), torch.zeros_like(t["fx"])
+        F.ic2d_passive_sums(gpu_ctx, vu, None, t["vx"], t["fx"], t["fz"], t["fa"], t["fm"], eps)
+        F.ic2d_passive_sums(gpu_ctx, fu, None, t["fx"], t["fx"], t["fz"], t["fa"], t["fm"], eps)
+        h = C.c_void_p()
+        core.check(core.lib().lpm_bve_rk4_create(gpu_ctx.handle, C.byref(h), vx.shape[0],
+                                                 fx.shape[0], dt, 2 * math.pi, eps,
+                                                 core.FP64_CHORD, flags))
+        ff = FarField(ctx=gpu_ctx)
+        keep.append(ff)
+        core.check(core.lib().lpm_bve_rk4_set_farfield(h, ff.handle, every))
+        for _ in range(3):
+            core.check(core.lib().lpm_bve_rk4_advance_timestep(
+                h, core.view(t["vx"]), core.ptr(t["vz"]), core.view(vu), core.view(t["fx"]),
+                core.ptr(t["fz"]), core.view(fu), core.ptr(t["fa"]), core.ptr(t["fm"])))
+        torch.cuda.synchronize()
+        out.append(fu.cpu().numpy()[fm == 0])
+        core.lib().lpm_bve_rk4_destroy(h)
+    assert _rel_linf(out[1], out[0]) < 2e-3
