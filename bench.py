@@ -683,6 +683,130 @@ def run_plane(args, device):
                                  "kinetic_energy": inv[2]},
             "clocks": clocks, "gpu_launches": ctx.kernel_launches - l0}
 
+# credited FP64 flops of the spherical SWE pair as evaluated (FMA = 2, the
+# reciprocal = 1): x.y 5, D 2, 1/D 1, scalings 6, c 9, w 6, v 3, velocity 12,
+# [y]x and P sums 8, rank-2 gradient update 6 + 36
+SWE_FLOPS_PER_PAIR = 94
+
+
+def run_swe(args, device):
+    """Spherical shallow-water direct sums (SphereVertexSums + SphereFaceSums,
+    src/lpm_swe_kernels.hpp:723-940): icosahedral level --swe-level, every
+    vertex and every face slot a target (as the functors launch), leaf faces
+    the sources, vorticity 2 Omega z + Rossby-Haurwitz-like wave, divergence
+    a smooth seeded field, eps = 0.01; FP64.  A step is one vertex + one face
+    evaluation (velocity and the double dot product).  Accuracy: against the
+    FP64 oracle on 2,048 seeded vertex targets."""
+    import torch
+
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+    level, eps = args.swe_level, 0.01
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
+    zeta = 2 * OMEGA * fx[:, 2] + 0.5 * fx[:, 2] * (1 - fx[:, 2] ** 2) ** 2 * np.cos(
+        4 * np.arctan2(fx[:, 1], fx[:, 0]))
+    sigma = 0.2 * np.sin(3 * fx[:, 0]) * fx[:, 1] + 0.05 * np.random.default_rng(7).standard_normal(fx.shape[0])
+    d = torch.device("cuda", device)
+    T = {k: torch.tensor(v, device=d) for k, v in
+         dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma).items()}
+    nv, ntot, nleaf = vx.shape[0], fx.shape[0], int((fm == 0).sum())
+    pairs = (nv + ntot) * nleaf
+    ov = F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps)
+    of = F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps)
+
+    def step():
+        F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                 out=ov)
+        F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps, out=of)
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(device)
+    fma64 = ctx.fma_peak_tflops(core.FP64)
+    sampler = ClockSampler(device)
+    sampler.start()
+    l0 = ctx.kernel_launches
+    ms = 0.0
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        ms += a.elapsed_time(b)
+    clocks = sampler.stop()
+    launches = ctx.kernel_launches - l0
+    pairs_per_s = pairs * args.steps / (ms * 1e-3)
+    # end to end: host inputs in, velocity + ddot out, every step
+    host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
+            dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma).items()}
+    h_out = [torch.empty(nv, 3, dtype=torch.float64).pin_memory(),
+             torch.empty(nv, dtype=torch.float64).pin_memory(),
+             torch.empty(ntot, 3, dtype=torch.float64).pin_memory(),
+             torch.empty(ntot, dtype=torch.float64).pin_memory()]
+    bi = sum(t.numel() * t.element_size() for t in host.values())
+    bo = sum(t.numel() * t.element_size() for t in h_out)
+    ms_e2e = 0.0
+    for k in range(max(1, args.steps // 2)):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for key, t in host.items():
+            T[key].copy_(t, non_blocking=True)
+        step()
+        for dst, src in zip(h_out, (ov["u"], ov["ddot"], of["u"], of["ddot"])):
+            dst.copy_(src, non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        ms_e2e += a.elapsed_time(b)
+    e2e = pairs * max(1, args.steps // 2) / (ms_e2e * 1e-3) / 1e9
+    # accuracy against the oracle and the CPU baseline on the same sample
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import lpm_oracle
+
+    threads = os.cpu_count() or 1
+    lpm_oracle.set_threads(threads)
+    idx = np.sort(np.random.default_rng(20261203).choice(nv, min(2048, nv), replace=False))
+    t0 = time.perf_counter()
+    ref = lpm_oracle.swe_sphere_sums(vx[idx], fx, zeta, sigma, fa, fm, eps)
+    cpu_s = time.perf_counter() - t0
+    got_u = ov["u"].cpu().numpy()[idx]
+    got_d = ov["ddot"].cpu().numpy()[idx]
+    ref_d = lpm_oracle.double_dot(ref[:, 3:])
+    err = {"velocity_linf": float(np.abs(got_u - ref[:, :3]).max() / np.abs(ref[:, :3]).max()),
+           "ddot_linf": float(np.abs(got_d - ref_d).max() / np.abs(ref_d).max())}
+    ach = pairs_per_s * SWE_FLOPS_PER_PAIR / 1e12
+    return {"metric": "spherical SWE direct sums Ginteractions/s (FP64, velocity + double dot)",
+            "value": round(pairs_per_s / 1e9, 4), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (generated icosahedral mesh, analytic + seeded fields)",
+            "config": {"workload": f"spherical SWE vertex + face sums, icosahedral level {level}, "
+                                   f"eps={eps}", "vertices": nv, "face_slots": ntot,
+                       "leaf_faces": nleaf, "interactions_per_step": pairs,
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": bi,
+                    "d2h_bytes_per_step": bo},
+            "roofline": {"bound": "fp64", "achieved": round(ach, 4), "peak": round(fma64, 4),
+                         "unit": "TFLOP/s", "frac": round(ach / fma64, 4),
+                         "traffic": None, "kernel": "k_swe_sphere (whole step timed)",
+                         "flops_per_pair_credited": SWE_FLOPS_PER_PAIR,
+                         "peak_kind": "measured FP64 FMA peak (lpm_measure_fma_peak)"},
+            "errors_vs_fp64_oracle_2048_vertex_targets": err,
+            "cpu_baseline": {"value": round(idx.size * nleaf / cpu_s / 1e9, 5), "unit": UNIT,
+                             "cores": threads, "kind": "port",
+                             "sample": f"{idx.size} vertex targets x {nleaf} leaf faces"},
+            "clocks": clocks, "gpu_launches": launches}
+
 
 def run_c5(args, device):
     """Configuration C5: BVE sphere at icosahedral level 8 (1,310,720 leaf
@@ -861,10 +985,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--level", type=int, default=LEVEL)
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5", "swe"], default="c2",
                     help="c2: the metric's workload (default); c1: FP64 level 4; "
                          "c3: planar dipoles; c4: 256-problem ensemble; "
-                         "c5: level 8 on the learned octree far field")
+                         "c5: level 8 on the learned octree far field; "
+                         "swe: spherical shallow-water sums (FP64)")
+    ap.add_argument("--swe-level", type=int, default=6)
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
     ap.add_argument("--ff-rho-min", type=float, default=0.25,
@@ -903,6 +1029,8 @@ def main():
         res = run_c1(args, local) if rank == 0 else {}
     elif args.config == "c5":
         res = run_c5(args, local) if rank == 0 else {}
+    elif args.config == "swe":
+        res = run_swe(args, local) if rank == 0 else {}
     else:
         res = run_ours(args, rank, world, local)
     if rank == 0:

@@ -321,8 +321,9 @@ int lpm_swe_plane_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot,
                               const double* fsigma, const double* farea,
                               const uint8_t* fmask, const double* fs, int64_t nf,
                               double eps, double pse_eps, int do_velocity);
-/* PlanarSWEFaceSums (:787-876): the same at every face slot; for eps == 0 the
- * i == j pair is skipped (collocated = !(eps > 0)). */
+/* PlanarSWEFaceSums (:787-876): the same at every face slot; for
+ * |eps| < DBL_EPSILON the i == j pair is skipped (collocated =
+ * FloatingPoint<Real>::zero(eps)). */
 int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
                             double* du1dx1, double* du1dx2, double* du2dx1,
                             double* du2dx2, double* laps, double* psi,
@@ -330,6 +331,29 @@ int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
                             const double* fsigma, const double* farea,
                             const uint8_t* fmask, const double* fs, int64_t nf,
                             double eps, double pse_eps, int do_velocity);
+
+/* ---- spherical shallow-water direct sums --------------------------------- */
+/* SphereVertexSums (src/lpm_swe_kernels.hpp:723-785): at nv vertices vx
+ * (nv x 3), from the face slots fx/fzeta/fsigma/farea/fmask (nf): velocity u
+ * (nv x 3, written if do_velocity) of kzeta_sphere + ksigma_sphere and the
+ * double dot product sum_ij M_ij M_ji of the summed gradient tensor
+ * M = sum_j grad_kzeta rot_j + grad_ksigma pot_j (rot = -zeta A,
+ * pot = -sigma A; sphere_swe_velocity_sums, :335-373).  grad, if not NULL,
+ * receives M itself (nv x 9, row-major, contiguous).  FP64; masked faces are
+ * skipped. */
+int lpm_swe_sphere_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot,
+                               double* grad, lpm_view vx, int64_t nv,
+                               lpm_view fx, const double* fzeta,
+                               const double* fsigma, const double* farea,
+                               const uint8_t* fmask, int64_t nf, double eps,
+                               int do_velocity);
+/* SphereFaceSums (:877-940): the same at every face slot; for
+ * |eps| < DBL_EPSILON the i == j pair is skipped. */
+int lpm_swe_sphere_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
+                             double* grad, lpm_view fx, const double* fzeta,
+                             const double* fsigma, const double* farea,
+                             const uint8_t* fmask, int64_t nf, double eps,
+                             int do_velocity);
 
 /* ---- octree far field with a learned correction ------------------------- */
 /* No reference counterpart: the reference's octree sources (LpmOctree*,

@@ -63,7 +63,7 @@ EXPORTS = [
     "lpm_farfield_set_network", "lpm_farfield_get_weights", "lpm_farfield_set_weights",
     "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
     "lpm_octree_stats", "lpm_mesh_build_device", "lpm_swe_plane_vertex_sums",
-    "lpm_swe_plane_face_sums",
+    "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
 ]
 
 
@@ -159,6 +159,8 @@ def _declare(L: C.CDLL) -> None:
                                       vp, vp, vp, i64, dbl, dbl, i32],
         "lpm_swe_plane_face_sums": [vp, V, vp, vp, vp, vp, vp, vp, vp, vp, V, vp, vp, vp, vp, vp,
                                     i64, dbl, dbl, i32],
+        "lpm_swe_sphere_vertex_sums": [vp, V, vp, vp, V, i64, V, vp, vp, vp, vp, i64, dbl, i32],
+        "lpm_swe_sphere_face_sums": [vp, V, vp, vp, V, vp, vp, vp, vp, i64, dbl, i32],
     }
     for name, args in sig.items():
         f = getattr(L, name)

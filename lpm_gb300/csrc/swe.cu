@@ -1,5 +1,7 @@
-// swe.cu -- planar shallow-water direct sums with particle strength exchange
-// (PlanarSWEVertexSums / PlanarSWEFaceSums, src/lpm_swe_kernels.hpp:626-876).
+// swe.cu -- shallow-water direct sums: planar with particle strength exchange
+// (PlanarSWEVertexSums / PlanarSWEFaceSums, src/lpm_swe_kernels.hpp:626-876)
+// and spherical (SphereVertexSums / SphereFaceSums, :723-940; see
+// k_swe_sphere below).
 //
 // Pair term (planar_swe_sums_rhs_pse, :394-480): with d = x - y,
 // R = |d|^2 + eps^2, rot = zeta A, pot = sigma A,
@@ -152,7 +154,205 @@ __global__ void k_swe_out(const double* __restrict__ part, int nchunks, int64_t 
   o.phi[i] = s[8];
 }
 
+// ---- spherical SWE sums ----------------------------------------------------
+// Pair term (sphere_swe_velocity_sums, :335-373) with s = x.y,
+// D = (1 - s) + eps^2, c = x cross y, rot = -zeta A, pot = -sigma A, and
+// P = I - x x^T:
+//   u += c rot / (4 pi D) + P y pot / (4 pi D)
+//   M += gkz rot + gks pot, where the reference's polynomials for grad_kzeta
+//   and grad_ksigma (:114-325) equal, over 4 pi D^2 (gkz identically, gks on
+//   the unit sphere),
+//     gkz = D [y]x + c v^T,          v = (1 + eps^2) x - y
+//     gks = -v w^T - D s P,          w = P y = y - s x
+//   (w - D x = -v because s + D = 1 + eps^2).
+// Per target the terms linear in [y]x and P are summed as a vector and a
+// scalar and applied once:
+//   M = sum_j (R c) v^T - (Q v) w^T + [sum_j rot y / (4 pi D)]x
+//       - (sum_j s pot / (4 pi D)) P,      R, Q = rot, pot / (4 pi D^2).
+// FP64: s and D = (1 - s) + eps^2 unfused in the reference's order (D is
+// the ill-conditioned quantity: a one-ulp change of s moves a near pair's D by
+// ~1e-16 / D relative), everything after it contracted, one reciprocal of D per
+// pair (Newton-Raphson from an FP32 seed, two steps: relative error below
+// 1e-28 before the final rounding); about 66 FP64 instructions per pair
+// against ~210 for the non-contracted three-division form.  Agreement with
+// the oracle (which keeps the reference's operation order) is ~1e-14
+// relative.
+constexpr int kSphNC = 16;  // u[3], Mr[9], Yd[3], G
+
+struct SphSrc {
+  double x, y, z, rot, pot;
+  int slot, pad;
+};
+
+__global__ void k_swe_sphere_pack(View fx, const double* __restrict__ zeta,
+                                  const double* __restrict__ sigma, const double* __restrict__ area,
+                                  const int* __restrict__ src2slot, int64_t ns,
+                                  SphSrc* __restrict__ src) {
+  const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = src2slot[k];
+  SphSrc r;
+  r.x = fx(j, 0);
+  r.y = fx(j, 1);
+  r.z = fx(j, 2);
+  r.rot = -zeta[j] * area[j];
+  r.pot = -sigma[j] * area[j];
+  r.slot = int(j);
+  r.pad = 0;
+  src[k] = r;
+}
+
+// 1/d by Newton-Raphson, r <- r + r (1 - d r), from the FP32 reciprocal.
+__device__ __forceinline__ double recip_nr(double d) {
+  double r = double(__frcp_rn(float(d)));
+  r = fma(r, fma(-d, r, 1.0), r);
+  return fma(r, fma(-d, r, 1.0), r);
+}
+
+__global__ void __launch_bounds__(kSweNT) k_swe_sphere(View tx, int64_t nt,
+                                                       const SphSrc* __restrict__ src, int64_t ns,
+                                                       int64_t chunk_len, double eps,
+                                                       int collocated, double* __restrict__ part,
+                                                       int64_t tpad) {
+  __shared__ SphSrc tile[kSweTile];
+  const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
+  const bool valid = i < nt;
+  double x[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) x[a] = valid ? tx(i, a) : 0.0;
+  const double epssq = eps * eps;
+  const double e1 = 1.0 + epssq;
+  const double inv4pi = 1.0 / (4 * kPI);
+  const double ex[3] = {e1 * x[0], e1 * x[1], e1 * x[2]};
+  double r[kSphNC];
+#pragma unroll
+  for (int k = 0; k < kSphNC; ++k) r[k] = 0.0;
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+    const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += kSweNT) tile[q] = src[t0 + q];
+    __syncthreads();
+    if (!valid) continue;
+#pragma unroll 2
+    for (int q = 0; q < m; ++q) {
+      const SphSrc& sr = tile[q];
+      if (collocated && sr.slot == i) continue;
+      const double y[3] = {sr.x, sr.y, sr.z};
+      // x.y unfused in the reference's order: D = 1 - s cancels, and its
+      // rounding is the reference's
+      const double s = da(da(dm(x[0], y[0]), dm(x[1], y[1])), dm(x[2], y[2]));
+      const double D = da(ds(1.0, s), epssq);
+      const double rd = recip_nr(D);
+      const double inv1 = rd * inv4pi;  // 1 / (4 pi D)
+      const double den2 = inv1 * rd;    // 1 / (4 pi D^2)
+      const double sz = sr.rot * inv1, ss = sr.pot * inv1;
+      const double R = sr.rot * den2, Q = sr.pot * den2;
+      const double cr[3] = {fma(x[1], y[2], -x[2] * y[1]), fma(x[2], y[0], -x[0] * y[2]),
+                            fma(x[0], y[1], -x[1] * y[0])};
+      double w[3], v[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        w[a] = fma(-s, x[a], y[a]);
+        v[a] = ex[a] - y[a];
+        r[a] = fma(cr[a], sz, fma(w[a], ss, r[a]));
+        r[12 + a] = fma(sz, y[a], r[12 + a]);
+      }
+      r[15] = fma(ss, s, r[15]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double al = R * cr[a], be = Q * v[a];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) r[3 + 3 * a + b] = fma(al, v[b], fma(-be, w[b], r[3 + 3 * a + b]));
+      }
+    }
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int k = 0; k < kSphNC; ++k) part[(c * kSphNC + k) * tpad + i] = r[k];
+}
+
+__global__ void k_swe_sphere_out(const double* __restrict__ part, int nchunks, int64_t tpad,
+                                 View tx, int64_t nt, View u, double* __restrict__ ddot,
+                                 double* __restrict__ grad, int do_velocity) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  double s[kSphNC];
+#pragma unroll
+  for (int k = 0; k < kSphNC; ++k) s[k] = 0.0;
+  for (int c = 0; c < nchunks; ++c)
+#pragma unroll
+    for (int k = 0; k < kSphNC; ++k) s[k] += part[(int64_t(c) * kSphNC + k) * tpad + i];
+  if (do_velocity) {
+    u(i, 0) = s[0];
+    u(i, 1) = s[1];
+    u(i, 2) = s[2];
+  }
+  const double x[3] = {tx(i, 0), tx(i, 1), tx(i, 2)};
+  const double* Yd = s + 12;
+  const double Yx[9] = {0.0, -Yd[2], Yd[1], Yd[2], 0.0, -Yd[0], -Yd[1], Yd[0], 0.0};
+  double M[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const double P = (a == b ? 1.0 : 0.0) - x[a] * x[b];
+      M[3 * a + b] = s[3 + 3 * a + b] + Yx[3 * a + b] - s[15] * P;
+    }
+  // sum_ij M_ij M_ji in the functors' loop order
+  double dsum = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) dsum = da(dsum, dm(M[3 * a + b], M[3 * b + a]));
+  ddot[i] = dsum;
+  if (grad)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) grad[9 * i + k] = M[k];
+}
+
+// Targets tx (nt x 3); sources: face slots fx/zeta/sigma/area/mask (nf);
+// collocated: targets are the face slots themselves (i == j skipped).
+void swe_sphere_sums(lpm_context& ctx, View tx, int64_t nt, View fx, const double* zeta,
+                     const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
+                     double eps, bool collocated, View u, double* ddot, double* grad,
+                     int do_velocity) {
+  if (nt == 0) return;
+  ctx.arena.reset();
+  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
+  const int64_t tpad = nb * kSweNT;
+  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
+  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
+  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
+                    sizeof(SphSrc) * size_t(nf) + sizeof(double) * kSphNC * size_t(nch_max) * tpad +
+                    8 * 4096);
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
+  SphSrc* src = static_cast<SphSrc*>(ctx.arena.take(sizeof(SphSrc) * std::max<int64_t>(ns, 1)));
+  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
+  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
+  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSphNC * size_t(nchunks) * tpad));
+  if (ns > 0) {
+    k_swe_sphere_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
+                                                                           src2slot, ns, src);
+    ctx.launches++;
+  }
+  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
+  k_swe_sphere<<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, ns, chunk_len, eps,
+                                                collocated ? 1 : 0, part, tpad);
+  k_swe_sphere_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, tx, nt,
+                                                                       u, ddot, grad, do_velocity);
+  ctx.launches += 2;
+  LPM_CUDA(cudaGetLastError());
+}
+
 bool bad_count(int64_t n) { return n < 0 || n > (int64_t(1) << 31) - 1; }
+
+// FloatingPoint<Real>::zero (src/util/lpm_floating_point.hpp:26-29): |x| < DBL_EPSILON
+bool fp_zero(double x) { return std::fabs(x) < 2.220446049250313e-16; }
 
 // Targets tx (nt x 2) with surface ts; sources: face slots fx/zeta/sigma/
 // area/mask/sfc (nf); collocated: targets are the face slots themselves.
@@ -248,9 +448,51 @@ int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot, double* 
   try {
     cudaSetDevice(ctx->device);
     lpm::SweOut o{lpm::to_view(u), ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, do_velocity};
-    // PlanarSWEFaceSums: collocated = !(eps > 0)
+    // PlanarSWEFaceSums: collocated = FloatingPoint<Real>::zero(eps)
     lpm::swe_plane_sums(*ctx, lpm::to_view(fx), fs, nf, lpm::to_view(fx), fzeta, fsigma, farea,
-                        fmask, fs, nf, eps, pse_eps, !(eps > 0), o);
+                        fmask, fs, nf, eps, pse_eps, lpm::fp_zero(eps), o);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_swe_sphere_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot, double* grad,
+                               lpm_view vx, int64_t nv, lpm_view fx, const double* fzeta,
+                               const double* fsigma, const double* farea, const uint8_t* fmask,
+                               int64_t nf, double eps, int do_velocity) {
+  if (!ctx) return lpm::fail(LPM_ERR_ARG, "null context");
+  if (lpm::bad_count(nv) || lpm::bad_count(nf))
+    return lpm::fail(LPM_ERR_ARG, "count out of range [0, 2^31-1]");
+  if (nv > 0 && (!vx.p || !ddot || (do_velocity && !u.p)))
+    return lpm::fail(LPM_ERR_ARG, "null target or output array");
+  if (nf > 0 && (!fx.p || !fzeta || !fsigma || !farea || !fmask))
+    return lpm::fail(LPM_ERR_ARG, "null source array");
+  if (!(eps >= 0) || !std::isfinite(eps)) return lpm::fail(LPM_ERR_ARG, "eps must be finite and >= 0");
+  try {
+    cudaSetDevice(ctx->device);
+    lpm::swe_sphere_sums(*ctx, lpm::to_view(vx), nv, lpm::to_view(fx), fzeta, fsigma, farea, fmask,
+                         nf, eps, false, lpm::to_view(u), ddot, grad, do_velocity);
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
+int lpm_swe_sphere_face_sums(lpm_context* ctx, lpm_view u, double* ddot, double* grad,
+                             lpm_view fx, const double* fzeta, const double* fsigma,
+                             const double* farea, const uint8_t* fmask, int64_t nf, double eps,
+                             int do_velocity) {
+  if (!ctx) return lpm::fail(LPM_ERR_ARG, "null context");
+  if (lpm::bad_count(nf)) return lpm::fail(LPM_ERR_ARG, "count out of range [0, 2^31-1]");
+  if (nf > 0 && (!fx.p || !fzeta || !fsigma || !farea || !fmask || !ddot || (do_velocity && !u.p)))
+    return lpm::fail(LPM_ERR_ARG, "null input or output array");
+  if (!(eps >= 0) || !std::isfinite(eps)) return lpm::fail(LPM_ERR_ARG, "eps must be finite and >= 0");
+  try {
+    cudaSetDevice(ctx->device);
+    // SphereFaceSums: collocated = FloatingPoint<Real>::zero(eps)
+    lpm::swe_sphere_sums(*ctx, lpm::to_view(fx), nf, lpm::to_view(fx), fzeta, fsigma, farea, fmask,
+                         nf, eps, lpm::fp_zero(eps), lpm::to_view(u), ddot, grad, do_velocity);
     return LPM_OK;
   } catch (...) {
     return lpm::handle_exception();

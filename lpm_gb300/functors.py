@@ -124,6 +124,40 @@ def swe_plane_face_sums(ctx, fx, fzeta, fsigma, farea, fmask, fs, eps, pse_eps, 
     return o
 
 
+def _sphere_swe_outputs(n, like, want_grad):
+    import torch
+
+    out = {"u": torch.zeros(n, 3, dtype=torch.float64, device=like.device),
+           "ddot": torch.zeros(n, dtype=torch.float64, device=like.device)}
+    if want_grad:
+        out["grad"] = torch.zeros(n, 9, dtype=torch.float64, device=like.device)
+    return out
+
+
+def swe_sphere_vertex_sums(ctx, vx, fx, fzeta, fsigma, farea, fmask, eps, do_velocity=True,
+                           want_grad=False, out=None):
+    """SphereVertexSums (src/lpm_swe_kernels.hpp:723-785): dict with u (n x 3),
+    ddot (n) and, if want_grad, the summed gradient tensor (n x 9, row-major).
+    `out` reuses a dict from an earlier call (u keeps its values when
+    do_velocity is false)."""
+    o = out if out is not None else _sphere_swe_outputs(_n(vx), vx, want_grad)
+    check(lib().lpm_swe_sphere_vertex_sums(
+        ctx.handle, view(o["u"]), ptr(o["ddot"]), ptr(o.get("grad")), view(vx), _n(vx), view(fx),
+        ptr(fzeta), ptr(fsigma), ptr(farea), ptr(fmask), _n(fx), eps, int(do_velocity)))
+    return o
+
+
+def swe_sphere_face_sums(ctx, fx, fzeta, fsigma, farea, fmask, eps, do_velocity=True,
+                         want_grad=False, out=None):
+    """SphereFaceSums (src/lpm_swe_kernels.hpp:877-940): as swe_sphere_vertex_sums
+    at every face slot (i == j skipped for |eps| < DBL_EPSILON)."""
+    o = out if out is not None else _sphere_swe_outputs(_n(fx), fx, want_grad)
+    check(lib().lpm_swe_sphere_face_sums(
+        ctx.handle, view(o["u"]), ptr(o["ddot"]), ptr(o.get("grad")), view(fx), ptr(fzeta),
+        ptr(fsigma), ptr(farea), ptr(fmask), _n(fx), eps, int(do_velocity)))
+    return o
+
+
 def ic2d_invariants(ctx, zeta, vel, area, mask):
     import ctypes as C
     out = (C.c_double * 3)()

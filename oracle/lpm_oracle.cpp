@@ -560,4 +560,77 @@ void oracle_swe_plane_sums(long nt, const double* tx, const double* ts, long ns,
   }
 }
 
+// Spherical SWE direct sums (SphereVertexSums / SphereFaceSums,
+// src/lpm_swe_kernels.hpp:723-940; pair term sphere_swe_velocity_sums
+// :335-373, reducer rules SphereSweDirectSumReducer :608-619).
+//
+// Pair term, with s = x.y, D = (1 - s) + eps^2, c = x cross y,
+// rot = -zeta A, pot = -sigma A:
+//   velocity (kzeta_sphere + ksigma_sphere, :63-108)
+//     u += c rot / (4 pi D) + (I - x x^T) y pot / (4 pi D)
+//   gradient (grad_kzeta, grad_ksigma, :114-325) -- the reference writes each
+//   entry as an expanded polynomial over 4 pi D^2; those polynomials equal
+//     gkz = (D [y]x + c ((1 + eps^2) x - y)^T) / (4 pi D^2)      (identically)
+//     gks = (w w^T - D (x w^T + s P)) / (4 pi D^2),  w = P y,  P = I - x x^T
+//   (on the unit sphere), i.e. gkz = -(dK_zeta/dx) P and gks = +(dK_sigma/dx) P
+//   for the kernels K_zeta = c / (4 pi D), K_sigma = P y / (4 pi D);
+//     M += gkz rot + gks pot  (9 entries, row-major).
+// The compact forms are used here; tests pin them against the reference's
+// polynomials evaluated in extended precision (tests/golden/).
+// Sums run in source order; masked sources are skipped, and with collocated
+// targets (face sums with |eps| < DBL_EPSILON) so is j == i.  The velocity
+// part follows the reference's operation order (velz + vels per pair); the
+// reference leaves the 3-vectors velz and vels of :341-346 uninitialised
+// before kzeta_sphere/ksigma_sphere add into them -- taken here as zero.
+// out12[12 i + k]: u, v, w, then M (du/dx, du/dy, du/dz, dv/dx, ...).
+void oracle_swe_sphere_sums(long nt, const double* tx, long ns, const double* y,
+                            const double* zeta, const double* sigma, const double* area,
+                            const unsigned char* mask, double eps, int collocated,
+                            double* out12) {
+  const double epssq = eps * eps;
+  const double e1 = 1 + epssq;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < nt; ++i) {
+    const double* x = tx + 3 * i;
+    double P[9];
+    for (int a = 0; a < 3; ++a) {
+      for (int b = 0; b < 3; ++b) P[3 * a + b] = -x[a] * x[b];
+      P[4 * a] += 1;
+    }
+    double r[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (long j = 0; j < ns; ++j) {
+      if (mask[j] || (collocated && i == j)) continue;
+      const double* yj = y + 3 * j;
+      const double s = sdot(x, yj);
+      const double D = 1 - s + epssq;
+      const double den1 = 4 * PI * D;
+      const double rot = -zeta[j] * area[j];
+      const double pot = -sigma[j] * area[j];
+      const double sz = rot / den1, ss = pot / den1;
+      double c[3];
+      scross(c, x, yj);
+      for (int a = 0; a < 3; ++a) {
+        double w = 0;
+        for (int b = 0; b < 3; ++b) w += P[3 * a + b] * yj[b];
+        r[a] += c[a] * sz + w * ss;
+      }
+      const double den2 = 1.0 / (4 * PI * ((1 - s + epssq) * (1 - s + epssq)));
+      const double Yx[9] = {0, -yj[2], yj[1], yj[2], 0, -yj[0], -yj[1], yj[0], 0};
+      double v[3], w[3];
+      for (int a = 0; a < 3; ++a) {
+        v[a] = e1 * x[a] - yj[a];
+        w[a] = yj[a] - s * x[a];
+      }
+      for (int a = 0; a < 3; ++a) {
+        for (int b = 0; b < 3; ++b) {
+          const double gkz = (D * Yx[3 * a + b] + c[a] * v[b]) * den2;
+          const double gks = (w[a] * w[b] - D * (x[a] * w[b] + s * P[3 * a + b])) * den2;
+          r[3 + 3 * a + b] += gkz * rot + gks * pot;
+        }
+      }
+    }
+    for (int k = 0; k < 12; ++k) out12[12 * i + k] = r[k];
+  }
+}
+
 }  // extern "C"

@@ -35,6 +35,7 @@ def lib() -> C.CDLL:
         sig = {
             "oracle_set_threads": [i],
             "oracle_swe_plane_sums": [l, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, i, vp],
+            "oracle_swe_sphere_sums": [l, vp, l, vp, vp, vp, vp, vp, d, i, vp],
             "oracle_set_sphere_form": [i],
             "oracle_max_threads": [],
             "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
@@ -194,6 +195,28 @@ def swe_plane_sums(tx, ts, y, zeta, sigma, area, mask, ss, eps, pse_eps, colloca
     lib().oracle_swe_plane_sums(tx.shape[0], _p(tx), _p(ts), y.shape[0], _p(y), _p(zeta),
                                 _p(sigma), _p(area), _p(mask), _p(ss), float(eps),
                                 float(pse_eps), int(collocated), _p(out))
+    return out
+
+
+def swe_sphere_sums(tx, y, zeta, sigma, area, mask, eps, collocated=False):
+    """Spherical SWE sums (n x 12): u, v, w and the velocity-gradient tensor
+    (row-major) of SphereVertexSums / SphereFaceSums."""
+    tx, y = _f(tx), _f(y)
+    zeta, sigma, area = _f(zeta), _f(sigma), _f(area)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros((tx.shape[0], 12))
+    lib().oracle_swe_sphere_sums(tx.shape[0], _p(tx), y.shape[0], _p(y), _p(zeta), _p(sigma),
+                                 _p(area), _p(mask), float(eps), int(collocated), _p(out))
+    return out
+
+
+def double_dot(m9):
+    """sum_ij M_ij M_ji in the functors' loop order (src/lpm_swe_kernels.hpp:777-782)."""
+    m9 = np.asarray(m9, np.float64)
+    out = np.zeros(m9.shape[0])
+    for a in range(3):
+        for b in range(3):
+            out = out + m9[:, 3 * a + b] * m9[:, 3 * b + a]
     return out
 
 

@@ -80,3 +80,130 @@ def test_swe_do_velocity_false_keeps_u(gpu_ctx):
         check(lib().lpm_swe_plane_face_sums(gpu_ctx.handle, view(u), *(ptr(o) for o in outs),
                                             view(T["fx"]), ptr(T["z"]), ptr(T["sg"]), ptr(T["fa"]),
                                             ptr(T["fm"]), ptr(T["fs"]), fx.shape[0], 0.05, 0.0, 1))
+
+
+# ---- spherical SWE sums ------------------------------------------------------
+
+def _sphere_fields(level, seed=5):
+    from lpm_gb300 import core
+
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
+    rng = np.random.default_rng(seed)
+    zeta = 2 * fx[:, 2] + np.sin(3 * fx[:, 0]) + 0.1 * rng.standard_normal(fx.shape[0])
+    sigma = np.cos(2 * fx[:, 2]) * fx[:, 1] + 0.1 * rng.standard_normal(fx.shape[0])
+    return vx, fx, fa, fm, zeta, sigma
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+def _dev(gpu_ctx, **arrays):
+    import torch
+
+    d = torch.device("cuda", gpu_ctx.device)
+    return {k: torch.tensor(v, device=d) for k, v in arrays.items()}
+
+
+@pytest.mark.parametrize("eps,tag", [(0.0, "e0"), (0.05, "e5")])
+def test_swe_sphere_golden(gpu_ctx, oracle, eps, tag):
+    """Against the reference's pair polynomials in extended precision
+    (tests/golden/swe_sphere_icos_l3.npz)."""
+    import torch
+    from pathlib import Path
+
+    from lpm_gb300 import functors as F
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "swe_sphere_icos_l3.npz")
+    T = _dev(gpu_ctx, vx=g["vx"], fx=g["fx"], fa=g["fa"], fm=g["fm"], z=g["zeta"], s=g["sigma"])
+    gv = F.swe_sphere_vertex_sums(gpu_ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                  want_grad=True)
+    gf = F.swe_sphere_face_sums(gpu_ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                want_grad=True)
+    torch.cuda.synchronize()
+    ft = g["face_targets"]
+    for o, ref, sel in ((gv, g[f"vert_{tag}"], slice(None)), (gf, g[f"face_{tag}"], ft)):
+        u = o["u"].cpu().numpy()[sel]
+        m = o["grad"].cpu().numpy()[sel]
+        dd = o["ddot"].cpu().numpy()[sel]
+        assert _rel(u, ref[:, :3]) < 1e-13
+        assert _rel(m, ref[:, 3:]) < 1e-12
+        assert _rel(dd, oracle.double_dot(ref[:, 3:])) < 1e-12
+
+
+@pytest.mark.parametrize("eps", [0.0, 0.02])
+def test_swe_sphere_parity(gpu_ctx, oracle, eps):
+    """Icosahedral level 5 vertices and level 4 faces (all slots, masked
+    parents excluded as sources) against the FP64 oracle."""
+    import torch
+
+    from lpm_gb300 import functors as F
+
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(5)
+    T = _dev(gpu_ctx, vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    gv = F.swe_sphere_vertex_sums(gpu_ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                  want_grad=True)
+    torch.cuda.synchronize()
+    rv = oracle.swe_sphere_sums(vx, fx, zeta, sigma, fa, fm, eps)
+    assert _rel(gv["u"].cpu().numpy(), rv[:, :3]) < 1e-12
+    assert _rel(gv["grad"].cpu().numpy(), rv[:, 3:]) < 1e-12
+    assert _rel(gv["ddot"].cpu().numpy(), oracle.double_dot(rv[:, 3:])) < 1e-12
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(4)
+    T = _dev(gpu_ctx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    gf = F.swe_sphere_face_sums(gpu_ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                want_grad=True)
+    torch.cuda.synchronize()
+    rf = oracle.swe_sphere_sums(fx, fx, zeta, sigma, fa, fm, eps, collocated=eps == 0)
+    leaf = fm == 0  # a parent slot coincides with its central child: 1/0 there
+    got_u = gf["u"].cpu().numpy()
+    assert np.array_equal(np.isfinite(got_u), np.isfinite(rf[:, :3]))
+    assert _rel(got_u[leaf], rf[leaf, :3]) < 1e-12
+    assert _rel(gf["grad"].cpu().numpy()[leaf], rf[leaf, 3:]) < 1e-12
+    assert _rel(gf["ddot"].cpu().numpy()[leaf], oracle.double_dot(rf[leaf, 3:])) < 1e-12
+
+
+def test_swe_sphere_views_and_flags(gpu_ctx, oracle):
+    """LayoutLeft-style strided views, do_velocity = 0 keeps u, no grad
+    pointer, all sources masked, zero targets, argument errors."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.core import check, lib, ptr, view
+
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(3)
+    T = _dev(gpu_ctx, vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    ref = F.swe_sphere_vertex_sums(gpu_ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"],
+                                   0.01)
+    # SoA with component stride nmax > n
+    def soa(a, extra=13):
+        buf = torch.zeros(3, a.shape[0] + extra, dtype=torch.float64, device=a.device)
+        buf[:, :a.shape[0]] = a.T
+        return buf[:, :a.shape[0]].T
+    vxs, fxs = soa(T["vx"]), soa(T["fx"])
+    us = soa(torch.zeros_like(T["vx"]))
+    o = {"u": us, "ddot": torch.zeros(vx.shape[0], dtype=torch.float64, device=us.device)}
+    F.swe_sphere_vertex_sums(gpu_ctx, vxs, fxs, T["z"], T["s"], T["fa"], T["fm"], 0.01, out=o)
+    torch.cuda.synchronize()
+    assert torch.equal(o["u"], ref["u"]) and torch.equal(o["ddot"], ref["ddot"])
+    # do_velocity = 0 leaves u alone, still writes ddot
+    o = {"u": torch.full_like(T["vx"], 7.0),
+         "ddot": torch.zeros(vx.shape[0], dtype=torch.float64, device=us.device)}
+    F.swe_sphere_vertex_sums(gpu_ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], 0.01,
+                             do_velocity=False, out=o)
+    torch.cuda.synchronize()
+    assert bool((o["u"] == 7.0).all()) and torch.equal(o["ddot"], ref["ddot"])
+    # every source masked: zeros
+    allm = torch.ones_like(T["fm"])
+    z = F.swe_sphere_face_sums(gpu_ctx, T["fx"], T["z"], T["s"], T["fa"], allm, 0.01)
+    torch.cuda.synchronize()
+    assert not bool(z["u"].any()) and not bool(z["ddot"].any())
+    # zero targets is a no-op
+    check(lib().lpm_swe_sphere_vertex_sums(gpu_ctx.handle, view(T["vx"]), ptr(o["ddot"]), None,
+                                           view(T["vx"]), 0, view(T["fx"]), ptr(T["z"]),
+                                           ptr(T["s"]), ptr(T["fa"]), ptr(T["fm"]), fx.shape[0],
+                                           0.0, 1))
+    with pytest.raises(core.LpmError):
+        check(lib().lpm_swe_sphere_face_sums(gpu_ctx.handle, view(T["fx"]), ptr(o["ddot"]), None,
+                                             view(T["fx"]), ptr(T["z"]), ptr(T["s"]), ptr(T["fa"]),
+                                             ptr(T["fm"]), fx.shape[0], -1.0, 1))
