@@ -75,6 +75,48 @@ inline void BVEFaceStreamFn(Context& c, double* psi, lpm_view fx, const double* 
   require(lpm_bve_face_stream_fn(c.get(), psi, fx, zeta, area, mask, nf), "BVEFaceStreamFn");
 }
 
+// ---- shallow-water sums (src/lpm_swe_kernels.hpp) --------------------------
+// PlanarSWEVertexSums / PlanarSWEFaceSums (:626-876)
+inline void PlanarSWEVertexSums(Context& c, lpm_view u, double* ddot, double* du1dx1,
+                                double* du1dx2, double* du2dx1, double* du2dx2, double* laps,
+                                double* psi, double* phi, lpm_view vx, const double* vs,
+                                int64_t nv, lpm_view fx, const double* zeta,
+                                const double* sigma, const double* area, const uint8_t* mask,
+                                const double* fs, int64_t nf, double eps, double pse_eps,
+                                bool do_velocity) {
+  require(lpm_swe_plane_vertex_sums(c.get(), u, ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi,
+                                    phi, vx, vs, nv, fx, zeta, sigma, area, mask, fs, nf, eps,
+                                    pse_eps, do_velocity ? 1 : 0),
+          "PlanarSWEVertexSums");
+}
+inline void PlanarSWEFaceSums(Context& c, lpm_view u, double* ddot, double* du1dx1,
+                              double* du1dx2, double* du2dx1, double* du2dx2, double* laps,
+                              double* psi, double* phi, lpm_view fx, const double* zeta,
+                              const double* sigma, const double* area, const uint8_t* mask,
+                              const double* fs, int64_t nf, double eps, double pse_eps,
+                              bool do_velocity) {
+  require(lpm_swe_plane_face_sums(c.get(), u, ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi,
+                                  phi, fx, zeta, sigma, area, mask, fs, nf, eps, pse_eps,
+                                  do_velocity ? 1 : 0),
+          "PlanarSWEFaceSums");
+}
+// SphereVertexSums / SphereFaceSums (:723-940); grad may be null
+inline void SphereVertexSums(Context& c, lpm_view u, double* ddot, lpm_view vx, int64_t nv,
+                             lpm_view fx, const double* zeta, const double* sigma,
+                             const double* area, const uint8_t* mask, double eps, int64_t nf,
+                             bool do_velocity, double* grad = nullptr) {
+  require(lpm_swe_sphere_vertex_sums(c.get(), u, ddot, grad, vx, nv, fx, zeta, sigma, area, mask,
+                                     nf, eps, do_velocity ? 1 : 0),
+          "SphereVertexSums");
+}
+inline void SphereFaceSums(Context& c, lpm_view u, double* ddot, lpm_view fx, const double* zeta,
+                           const double* sigma, const double* area, const uint8_t* mask,
+                           double eps, int64_t nf, bool do_velocity, double* grad = nullptr) {
+  require(lpm_swe_sphere_face_sums(c.get(), u, ddot, grad, fx, zeta, sigma, area, mask, nf, eps,
+                                   do_velocity ? 1 : 0),
+          "SphereFaceSums");
+}
+
 // ---- BVERK4 (src/lpm_bve_rk4.hpp:10-77) ----------------------------------
 class BVERK4 {
  public:
