@@ -355,6 +355,35 @@ int lpm_swe_sphere_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
                              const uint8_t* fmask, int64_t nf, double eps,
                              int do_velocity);
 
+/* ---- mesh connectivity and VTK output (host) ----------------------------- */
+/* Face vertex lists of the uniform mesh lpm_mesh_build makes: *nfv vertices
+ * per face slot (3 icosahedral, 4 cubed sphere / quad), counter-clockwise
+ * seen from outside (sphere) or from +z (plane), parents included.  With
+ * fverts == NULL only *nfv is set; otherwise fverts holds nfaces * nfv. */
+int lpm_mesh_face_vertices(int kind, int level, double radius, int* nfv,
+                           int32_t* fverts);
+
+/* One data array of a VTK file: location 0 = point data (one tuple per
+ * vertex), 1 = cell data (one tuple per face slot; leaf slots written);
+ * ncomp values per tuple, row-major. */
+typedef struct {
+  const char* name;
+  int location;
+  int ncomp;
+  const double* data;
+} lpm_vtk_field;
+
+/* VtkPolymeshInterface (src/vtk/lpm_vtk_io.hpp:36-76) without VTK: writes a
+ * VTK XML PolyData file (.vtp, ASCII, shortest round-trip decimals) of the
+ * vertices (points; z = height in the plane, (1 + height) x on the sphere
+ * when height is not NULL) and the leaf faces (polygons, slot order), cell
+ * array "area", then the fields in order.  All pointers are host memory. */
+int lpm_vtk_write_polymesh(const char* path, int ndim, int64_t nv,
+                           const double* vx, const double* height, int64_t nf,
+                           int nfv, const int32_t* fverts, const uint8_t* fmask,
+                           const double* farea, int nfields,
+                           const lpm_vtk_field* fields);
+
 /* ---- octree far field with a learned correction ------------------------- */
 /* No reference counterpart: the reference's octree sources (LpmOctree*,
  * LpmNodeArray*) are not built and src/tree/lpm_cpu_tree's generators are

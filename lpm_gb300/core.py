@@ -64,6 +64,7 @@ EXPORTS = [
     "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
     "lpm_octree_stats", "lpm_mesh_build_device", "lpm_swe_plane_vertex_sums",
     "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
+    "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh",
 ]
 
 
@@ -161,6 +162,8 @@ def _declare(L: C.CDLL) -> None:
                                     i64, dbl, dbl, i32],
         "lpm_swe_sphere_vertex_sums": [vp, V, vp, vp, V, i64, V, vp, vp, vp, vp, i64, dbl, i32],
         "lpm_swe_sphere_face_sums": [vp, V, vp, vp, V, vp, vp, vp, vp, i64, dbl, i32],
+        "lpm_mesh_face_vertices": [i32, i32, dbl, C.POINTER(i32), vp],
+        "lpm_vtk_write_polymesh": [C.c_char_p, i32, i64, vp, vp, i64, i32, vp, vp, vp, i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -268,6 +271,16 @@ def build_mesh(kind: int, level: int, radius: float = 1.0):
     fm = np.empty(nf, np.uint8)
     check(lib().lpm_mesh_build(kind, level, radius, ptr(vx), ptr(fx), ptr(fa), ptr(fm)))
     return vx, fx, fa, fm
+
+
+def mesh_face_vertices(kind: int, level: int, radius: float = 1.0) -> np.ndarray:
+    """Face vertex lists (nf x nfv, int32) of the mesh build_mesh makes."""
+    nfv = C.c_int32()
+    check(lib().lpm_mesh_face_vertices(kind, level, radius, C.byref(nfv), None))
+    _, nf = mesh_sizes(kind, level)
+    out = np.empty((nf, nfv.value), np.int32)
+    check(lib().lpm_mesh_face_vertices(kind, level, radius, C.byref(nfv), ptr(out)))
+    return out
 
 
 def build_mesh_device(ctx, kind: int, level: int, radius: float = 1.0):

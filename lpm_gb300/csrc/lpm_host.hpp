@@ -14,8 +14,10 @@ namespace lpm {
 
 // ---- host-only helpers (mesh.cpp, ics.cpp) --------------------------------
 void mesh_sizes(int kind, int level, int64_t* nv, int64_t* nf);
+// fverts (optional): nfv vertex indices per face slot, counter-clockwise
 void mesh_build(int kind, int level, double radius, double* vx, double* fx,
-                double* farea, uint8_t* fmask);
+                double* farea, uint8_t* fmask, int32_t* fverts = nullptr);
+int mesh_nfv(int kind);  // vertices per face of a mesh kind
 void ic_eval(int kind, const double* prm, int np, int ndim, int64_t n,
              const double* x, double* zeta);
 // Level-0 mesh (the seed) with its face vertex lists (nfv per face).

@@ -333,7 +333,7 @@ void mesh_seed(int kind, double radius, MeshSeed& out) {
 }
 
 void mesh_build(int kind, int level, double radius, double* vx, double* fx,
-                double* farea, uint8_t* fmask) {
+                double* farea, uint8_t* fmask, int32_t* fverts) {
   int64_t nv, nf;
   mesh_sizes(kind, level, &nv, &nf);
   Builder b;
@@ -358,6 +358,23 @@ void mesh_build(int kind, int level, double radius, double* vx, double* fx,
   std::memcpy(fx, b.fx.data(), sizeof(double) * b.fx.size());
   std::memcpy(farea, b.area.data(), sizeof(double) * b.area.size());
   std::memcpy(fmask, b.mask.data(), b.mask.size());
+  if (fverts) {
+    int64_t k = 0;
+    for (const auto& f : b.fverts)
+      for (int i = 0; i < b.nfv; ++i) fverts[k++] = int32_t(f[i]);
+  }
+}
+
+int mesh_nfv(int kind) {
+  switch (kind) {
+    case LPM_MESH_ICOS_TRI:
+      return 3;
+    case LPM_MESH_CUBED_SPHERE:
+    case LPM_MESH_QUAD_RECT:
+      return 4;
+    default:
+      throw std::invalid_argument("unknown mesh kind");
+  }
 }
 
 }  // namespace lpm
