@@ -496,7 +496,7 @@ void lpm_farfield::evaluate(const void* tgt, const void* src, double* wout, int6
   }
   ff_launch_tree(*ctx, *d, tgt, src, wout, wstride, c0, theta, rho_min, learn);
   if (timing) LPM_CUDA(cudaEventRecord(ev[1], ctx->stream));
-  if (learn) ff_launch_mlp(*ctx, *d, *net, wout, wstride, eps, rho_min);
+  if (learn) ff_launch_mlp(*ctx, *d, *net, norm.data(), wout, wstride, eps, rho_min);
   if (timing) LPM_CUDA(cudaEventRecord(ev[2], ctx->stream));
 }
 

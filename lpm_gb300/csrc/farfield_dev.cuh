@@ -52,7 +52,7 @@ void ff_cells(lpm_context& ctx, const float4* ys, const int4* cells, int ncells,
 // tcgen05 operand-layout self-test (device pointers, see mlp.cu).
 void tc_selftest(lpm_context& ctx, const float* A, const float* B, float* D, int N, int K, int amn,
                  int bmn);
-void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int64_t wstride,
-                   double eps, double rho_min);
+void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, const float* norm, double* wout,
+                   int64_t wstride, double eps, double rho_min);
 
 }  // namespace lpm

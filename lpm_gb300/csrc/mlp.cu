@@ -38,6 +38,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "f32x2.cuh"
 #include "farfield_dev.cuh"
 #include "ffmath.cuh"
 #include "nbody.cuh"
@@ -101,20 +102,37 @@ __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& ph) {
 
 // Bias + SiLU epilogue of one 128-column layer: TMEM lane row -> BF16 row of
 // the next operand (unit kBiasHid is the constant 1).
+// SiLU of a pair with packed FP32 arithmetic: h = z/2, silu(z) = h + h tanh(h)
+// (one mul.f32x2, two tanh.approx, one fma.f32x2), rounded to a BF16 pair.
+__device__ __forceinline__ uint32_t silu2_bf16(float a, float b) {
+  const u64 h = mul2(pk2(a, b), pk2(0.5f, 0.5f));
+  float h0, h1;
+  upk2(h, h0, h1);
+  const u64 y = fma2(h, pk2(ff::tanh_approx(h0), ff::tanh_approx(h1)), h);
+  float y0, y1;
+  upk2(y, y0, y1);
+  return tc::pack_bf16(y0, y1);
+}
+
+// The eight 16-column chunks are software-pipelined: the TMEM load of chunk
+// k + 1 is in flight while chunk k is activated and stored.
 __device__ __forceinline__ void silu_rows(uint32_t tacc, int warp, unsigned char* dst, int row) {
-#pragma unroll 1
-  for (int cc = 0; cc < kHid; cc += 16) {
-    float v[16];
-    tc::ld16(tc::lane_addr(tacc, warp, cc), v);
+  uint32_t r[2][16];
+  tc::ld16_issue(tc::lane_addr(tacc, warp, 0), r[0]);
+  tc::ld16_wait(r[0]);
+#pragma unroll
+  for (int k = 0; k < kHid / 16; ++k) {
+    uint32_t* cur = r[k & 1];
+    if (k + 1 < kHid / 16) tc::ld16_issue(tc::lane_addr(tacc, warp, 16 * (k + 1)), r[(k + 1) & 1]);
     uint32_t p[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      float a = ff::silu(v[2 * i]), b = ff::silu(v[2 * i + 1]);
-      if (cc + 2 * i + 1 == kBiasHid) b = 1.f;
-      p[i] = tc::pack_bf16(a, b);
-    }
-    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc, kHid)) = make_uint4(p[0], p[1], p[2], p[3]);
-    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, cc + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);
+    for (int i = 0; i < 8; ++i) p[i] = silu2_bf16(__uint_as_float(cur[2 * i]), __uint_as_float(cur[2 * i + 1]));
+    // unit kBiasHid (the last hidden unit) is the constant 1: BF16 0x3F80
+    static_assert(kBiasHid == kHid - 1, "bias unit is the last hidden unit");
+    if (k == kHid / 16 - 1) p[7] = (p[7] & 0xffffu) | 0x3f800000u;
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, 16 * k, kHid)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(dst + tc::cm_off(row, 16 * k + 8, kHid)) = make_uint4(p[4], p[5], p[6], p[7]);
+    if (k + 1 < kHid / 16) tc::ld16_wait(r[(k + 1) & 1]);
   }
 }
 
@@ -187,9 +205,7 @@ template <class SYNC>
 __device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t* bar, uint32_t& ph,
                                         const SYNC& s, int xo, int a1, int a2, int a3) {
   const int row = threadIdx.x & 127, w = threadIdx.x >> 5;
-  const int in_buf[3] = {xo, a1, a2};
-  const int out_buf[3] = {a1, a2, a3};
-  const int wts[3] = {kSmW1, kSmW2, kSmW3};
+  bool ok = true;
 #pragma unroll 1
   for (int l = 0; l < 3; ++l) {
     tc::fence_smem_async();
@@ -198,12 +214,15 @@ __device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t
     if (s.leader()) {
       tc::fence_after();
       const int k = l == 0 ? kIn : kHid;
-      gemm_kk(tb, sbase(sm, in_buf[l]), k * 16, sbase(sm, wts[l]), k * 16, kID128, k / 16);
+      const int in_buf = l == 0 ? xo : (l == 1 ? a1 : a2);
+      const int wts = l == 0 ? kSmW1 : (l == 1 ? kSmW2 : kSmW3);
+      gemm_kk(tb, sbase(sm, in_buf), k * 16, sbase(sm, wts), k * 16, kID128, k / 16);
       tc::commit(bar);
     }
-    const bool ok = wait_mma(bar, ph);
-    if (s.any(!ok)) return false;
-    silu_rows(tb, w, sm + out_buf[l], row);
+    // a timed-out wait is agreed on once, after the output layer: every
+    // later wait is bounded too, so all threads keep meeting the barriers
+    ok = wait_mma(bar, ph) && ok;
+    silu_rows(tb, w, sm + (l == 0 ? a1 : (l == 1 ? a2 : a3)), row);
   }
   tc::fence_smem_async();
   tc::fence_before();
@@ -213,7 +232,7 @@ __device__ __forceinline__ bool forward(unsigned char* sm, uint32_t tb, uint64_t
     gemm_kk(tb, sbase(sm, a3), kHid * 16, sbase(sm, kSmW4), kHid * 16, kID16, kHid / 16);
     tc::commit(bar);
   }
-  const bool ok = wait_mma(bar, ph);
+  ok = wait_mma(bar, ph) && ok;
   return !s.any(!ok);
 }
 
@@ -225,7 +244,9 @@ struct MlpArgs {
   const int* lrn;
   const int4* cnt;
   const uint16_t* wbf;
-  const float* norm;
+  // input normalisation f * nsc + nsh (nsc = 1/sd, nsh = -mean/sd) and the
+  // output scale, in the parameter space: constant-bank operands
+  float nsc[kIn], nsh[kIn], oscale;
   double* wout;
   int64_t wstride;
   float eps, rho_min;
@@ -247,10 +268,8 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   __shared__ uint64_t bar[kInfWG];
   __shared__ uint32_t tslot;
   __shared__ int blk[kInfWG];
-  __shared__ float nrm[2 * kIn + 1];
   const int t = threadIdx.x, w = t >> 5, g = t >> 7, lt = t & 127, lane = t & 31;
   load_weights(sm, a.wbf);
-  for (int i = t; i < 2 * kIn + 1; i += blockDim.x) nrm[i] = a.norm[i];
   if (t == 0) {
     for (int i = 0; i < kInfWG; ++i) mbar_init(&bar[i], 1);
     mbar_fence_init();
@@ -268,7 +287,7 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
   float4* contrib = reinterpret_cast<float4*>(sm + ho);  // over H after the output layer
   uint32_t ph = 0;
   bool ok = true;
-  const float oscale = nrm[2 * kIn];
+  const float oscale = a.oscale;
   const float rho_min = a.rho_min;
   for (;;) {
     s.sync();
@@ -308,7 +327,7 @@ __global__ void __launch_bounds__(128 * kInfWG, 1) k_ff_mlp(const MlpArgs a) {
 #pragma unroll
       for (int i = kBiasIn + 1; i < kIn; ++i) f[i] = 0.f;
 #pragma unroll
-      for (int i = 0; i < kIn; ++i) f[i] = have ? (f[i] - nrm[i]) * nrm[kIn + i] : 0.f;
+      for (int i = 0; i < kIn; ++i) f[i] = have ? fmaf(f[i], a.nsc[i], a.nsh[i]) : 0.f;
       write_x_row(sm + ho, lt, f);
       if (!forward(sm, tb, &bar[g], ph, s, ho, ho, ho, ho)) return false;
       float o[16];
@@ -833,8 +852,8 @@ void ff_prepare_kernels() {
   LPM_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTrain));
 }
 
-void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int64_t wstride,
-                   double eps, double rho_min) {
+void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, const float* norm, double* wout,
+                   int64_t wstride, double eps, double rho_min) {
   LPM_CUDA(cudaMemsetAsync(d.counter, 0, 4 * sizeof(int), ctx.stream));
   MlpArgs a;
   a.xt = d.xt;
@@ -844,7 +863,11 @@ void ff_launch_mlp(lpm_context& ctx, FFDevice& d, FFNet& net, double* wout, int6
   a.lrn = d.lrn;
   a.cnt = d.cnt;
   a.wbf = net.wbf;
-  a.norm = net.norm;
+  for (int i = 0; i < kIn; ++i) {
+    a.nsc[i] = norm[kIn + i];
+    a.nsh[i] = -norm[i] * norm[kIn + i];
+  }
+  a.oscale = norm[2 * kIn];
   a.wout = wout;
   a.wstride = wstride;
   a.eps = float(eps);

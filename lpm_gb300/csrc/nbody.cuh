@@ -33,6 +33,7 @@
 
 #include <cuda_runtime.h>
 
+#include "f32x2.cuh"
 #include "lpm_gb300.h"
 
 namespace lpm {
@@ -202,33 +203,6 @@ __host__ __device__ inline SrcF32 make_src_f32(float x, float y, float z, float 
 template <typename T> struct SrcRec;
 template <> struct SrcRec<float> { using type = SrcF32; };
 template <> struct SrcRec<double> { using type = double4; };
-
-// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction does the
-// operation on both halves of a 64-bit register pair.
-using u64 = unsigned long long;
-__device__ __forceinline__ u64 pk2(float lo, float hi) {
-  u64 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void upk2(u64 v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-  u64 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-  u64 d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-  u64 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
 
 __device__ __forceinline__ float chord_rcp(float q) { return rcp_approx(q); }
 __device__ __forceinline__ double chord_rcp(double q) { return 1.0 / q; }
