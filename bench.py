@@ -687,16 +687,22 @@ def run_plane(args, device):
 # reciprocal = 1): x.y 5, D 2, 1/D 1, scalings 6, c 9, w 6, v 3, velocity 12,
 # [y]x and P sums 8, rank-2 gradient update 6 + 36
 SWE_FLOPS_PER_PAIR = 94
+# FP32C form (chord moments): d from hi/lo parts 6, |d|^2 + c0 6, 1/q 1,
+# scalings 6, first moments 12 + 12, second moments 24, scalar sums 4
+SWE32_FLOPS_PER_PAIR = 71
 
 
 def run_swe(args, device):
     """Spherical shallow-water direct sums (SphereVertexSums + SphereFaceSums,
     src/lpm_swe_kernels.hpp:723-940): icosahedral level --swe-level, every
     vertex and every face slot a target (as the functors launch), leaf faces
-    the sources, vorticity 2 Omega z + Rossby-Haurwitz-like wave, divergence
-    a smooth seeded field, eps = 0.01; FP64.  A step is one vertex + one face
-    evaluation (velocity and the double dot product).  Accuracy: against the
-    FP64 oracle on 2,048 seeded vertex targets."""
+    the sources, vorticity 2 Omega z + a Rossby-Haurwitz-like wave, divergence
+    a smooth seeded field, eps = 0.01.  A step is one vertex + one face
+    evaluation (velocity and the double dot product).  `value` is the
+    FP32-compensated form (context precision FP32C); the FP64 form (the
+    reference's arithmetic) is timed on one step beside it.  Accuracy:
+    FP32C against the FP64 path on every leaf target; FP64 against the CPU
+    oracle on 2,048 seeded vertex targets."""
     import torch
 
     from lpm_gb300 import build as B
@@ -718,35 +724,47 @@ def run_swe(args, device):
          dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma).items()}
     nv, ntot, nleaf = vx.shape[0], fx.shape[0], int((fm == 0).sum())
     pairs = (nv + ntot) * nleaf
-    ov = F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps)
-    of = F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps)
+    outs = {p: (F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"],
+                                         eps),
+                F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps))
+            for p in (core.FP64, core.FP32C)}
 
-    def step():
+    def step(prec):
+        ctx.set_precision(prec)
+        ov, of = outs[prec]
         F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
                                  out=ov)
         F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps, out=of)
 
+    def timed(prec, n, flush_buf):
+        ms = 0.0
+        for k in range(n):
+            flush_buf.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(prec)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms += a.elapsed_time(b)
+        return ms
+
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    step(core.FP64)
+    torch.cuda.synchronize(device)
+    ms64 = timed(core.FP64, 1, flush)
     for _ in range(args.warmup):
-        step()
+        step(core.FP32C)
     torch.cuda.synchronize(device)
     fma64 = ctx.fma_peak_tflops(core.FP64)
+    peak32, sm_max, nsm = fp32_peak(device)
     sampler = ClockSampler(device)
     sampler.start()
     l0 = ctx.kernel_launches
-    ms = 0.0
-    for k in range(args.steps):
-        flush.fill_(float(k))
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        step()
-        b.record(stream)
-        torch.cuda.synchronize(device)
-        ms += a.elapsed_time(b)
+    ms = timed(core.FP32C, args.steps, flush)
     clocks = sampler.stop()
     launches = ctx.kernel_launches - l0
     pairs_per_s = pairs * args.steps / (ms * 1e-3)
-    # end to end: host inputs in, velocity + ddot out, every step
+    # end to end (FP32C): host inputs in, velocity + ddot out, every step
     host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in
             dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma).items()}
     h_out = [torch.empty(nv, 3, dtype=torch.float64).pin_memory(),
@@ -755,21 +773,30 @@ def run_swe(args, device):
              torch.empty(ntot, dtype=torch.float64).pin_memory()]
     bi = sum(t.numel() * t.element_size() for t in host.values())
     bo = sum(t.numel() * t.element_size() for t in h_out)
+    ov32, of32 = outs[core.FP32C]
     ms_e2e = 0.0
-    for k in range(max(1, args.steps // 2)):
+    n_e2e = max(1, args.steps // 2)
+    for k in range(n_e2e):
         flush.fill_(float(k))
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         for key, t in host.items():
             T[key].copy_(t, non_blocking=True)
-        step()
-        for dst, src in zip(h_out, (ov["u"], ov["ddot"], of["u"], of["ddot"])):
+        step(core.FP32C)
+        for dst, src in zip(h_out, (ov32["u"], ov32["ddot"], of32["u"], of32["ddot"])):
             dst.copy_(src, non_blocking=True)
         b.record(stream)
         torch.cuda.synchronize(device)
         ms_e2e += a.elapsed_time(b)
-    e2e = pairs * max(1, args.steps // 2) / (ms_e2e * 1e-3) / 1e9
-    # accuracy against the oracle and the CPU baseline on the same sample
+    e2e = pairs * n_e2e / (ms_e2e * 1e-3) / 1e9
+    # FP32C against FP64 on every leaf target (vertices and leaf faces)
+    ov64, of64 = outs[core.FP64]
+    leaf = T["fm"] == 0
+    err32 = {"velocity_vertices": rel_errors(ov32["u"], ov64["u"]),
+             "velocity_leaf_faces": rel_errors(of32["u"][leaf], of64["u"][leaf]),
+             "ddot_vertices": rel_errors(ov32["ddot"], ov64["ddot"]),
+             "ddot_leaf_faces": rel_errors(of32["ddot"][leaf], of64["ddot"][leaf])}
+    # FP64 against the CPU oracle, and the CPU baseline on the same sample
     sys.path.insert(0, str(ROOT / "oracle"))
     import lpm_oracle
 
@@ -779,32 +806,41 @@ def run_swe(args, device):
     t0 = time.perf_counter()
     ref = lpm_oracle.swe_sphere_sums(vx[idx], fx, zeta, sigma, fa, fm, eps)
     cpu_s = time.perf_counter() - t0
-    got_u = ov["u"].cpu().numpy()[idx]
-    got_d = ov["ddot"].cpu().numpy()[idx]
+    got_u = ov64["u"].cpu().numpy()[idx]
+    got_d = ov64["ddot"].cpu().numpy()[idx]
     ref_d = lpm_oracle.double_dot(ref[:, 3:])
-    err = {"velocity_linf": float(np.abs(got_u - ref[:, :3]).max() / np.abs(ref[:, :3]).max()),
-           "ddot_linf": float(np.abs(got_d - ref_d).max() / np.abs(ref_d).max())}
-    ach = pairs_per_s * SWE_FLOPS_PER_PAIR / 1e12
-    return {"metric": "spherical SWE direct sums Ginteractions/s (FP64, velocity + double dot)",
-            "value": round(pairs_per_s / 1e9, 4), "unit": UNIT, "n_gpus": 1,
+    err64 = {"velocity_linf": float(np.abs(got_u - ref[:, :3]).max() / np.abs(ref[:, :3]).max()),
+             "ddot_linf": float(np.abs(got_d - ref_d).max() / np.abs(ref_d).max())}
+    ach = pairs_per_s * SWE32_FLOPS_PER_PAIR / 1e12
+    ach64 = pairs / (ms64 * 1e-3) * SWE_FLOPS_PER_PAIR / 1e12
+    return {"metric": "spherical SWE direct sums Ginteractions/s (velocity + double dot)",
+            "value": round(pairs_per_s / 1e9, 3), "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (generated icosahedral mesh, analytic + seeded fields)",
             "config": {"workload": f"spherical SWE vertex + face sums, icosahedral level {level}, "
                                    f"eps={eps}", "vertices": nv, "face_slots": ntot,
                        "leaf_faces": nleaf, "interactions_per_step": pairs,
                        "l2": "flushed between timed steps (512 MiB write)"},
-            "e2e": {"value": round(e2e, 4), "unit": UNIT, "h2d_bytes_per_step": bi,
+            "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": bi,
                     "d2h_bytes_per_step": bo},
-            "roofline": {"bound": "fp64", "achieved": round(ach, 4), "peak": round(fma64, 4),
-                         "unit": "TFLOP/s", "frac": round(ach / fma64, 4),
-                         "traffic": None, "kernel": "k_swe_sphere (whole step timed)",
-                         "flops_per_pair_credited": SWE_FLOPS_PER_PAIR,
-                         "peak_kind": "measured FP64 FMA peak (lpm_measure_fma_peak)"},
-            "errors_vs_fp64_oracle_2048_vertex_targets": err,
+            "roofline": {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak32, 2),
+                         "unit": "TFLOP/s", "frac": round(ach / peak32, 4), "traffic": None,
+                         "kernel": "k_swe_sphere32 (whole step timed)",
+                         "flops_per_pair_credited": SWE32_FLOPS_PER_PAIR,
+                         "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"},
+            "fp64": {"value": round(pairs / (ms64 * 1e-3) / 1e9, 4), "unit": UNIT,
+                     "ms_per_step": round(ms64, 2),
+                     "roofline": {"bound": "fp64", "achieved": round(ach64, 4),
+                                  "peak": round(fma64, 4), "unit": "TFLOP/s",
+                                  "frac": round(ach64 / fma64, 4),
+                                  "flops_per_pair_credited": SWE_FLOPS_PER_PAIR,
+                                  "peak_kind": "measured FP64 FMA peak (lpm_measure_fma_peak)"}},
+            "errors_fp32c_vs_fp64_all_leaf_targets": err32,
+            "errors_fp64_vs_oracle_2048_vertex_targets": err64,
             "cpu_baseline": {"value": round(idx.size * nleaf / cpu_s / 1e9, 5), "unit": UNIT,
                              "cores": threads, "kind": "port",
-                             "sample": f"{idx.size} vertex targets x {nleaf} leaf faces"},
+                             "sample": f"{idx.size} vertex targets x {nleaf} leaf faces, FP64"},
             "clocks": clocks, "gpu_launches": launches}
 
 

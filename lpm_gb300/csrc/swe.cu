@@ -312,12 +312,251 @@ __global__ void k_swe_sphere_out(const double* __restrict__ part, int nchunks, i
     for (int k = 0; k < 9; ++k) grad[9 * i + k] = M[k];
 }
 
+// ---- spherical SWE sums, FP32 compensated (context precision LPM_FP32C) ----
+// Chord form: with d = x - y for unit vectors, 1 - x.y = |d|^2 / 2, so
+// D = q / 2 with q = |d|^2 + 2 eps^2, and c = x cross y = d cross x,
+// v = eps^2 x + d, w = P y = -P d.  Writing rs, ps = rot, pot / (2 pi) and
+// r = 1/q, the pair scalars are sz = rs r, ss = ps r (= rot, pot / (4 pi D))
+// and R = 2 sz r, Q = 2 ss r (= rot, pot / (4 pi D^2)).  Every term is then a
+// moment of d, summed per target (27 sums):
+//   A = sum sz d, B = sum ss d, U1 = sum R d, V1 = sum Q d,
+//   U2 = sum R d d^T, V2 = sum Q d d^T (symmetric), Z = sum sz, G = sum ss,
+//   H = sum ss |d|^2,
+// and the epilogue (FP64) assembles
+//   u = A x x - P B
+//   M = eps^2 (U1 x x) x^T + [U2 columns] x x + eps^2 x (P V1)^T + V2 P
+//       + [Z x - A]x - (G - H/2) P.
+// Positions are split into FP32 hi + lo parts so that d = (xh - yh) +
+// (xl - yl) carries its own FP32 rounding, not the positions' (near pairs
+// dominate the gradient: their |d| shrinks with the mesh).  Per-pair work is
+// FP32 with one MUFU reciprocal (~50 instructions); each 256-source tile's FP32
+// partials are merged into (sum, compensation) pairs by TwoSum.
+constexpr int kSph32NC = 27;  // A3 B3 U1[3] V1[3] U2[6] V2[6] Z G H
+
+struct __align__(16) SphSrc32 {
+  float4 hi;  // x, y, z, rot / (2 pi)
+  float4 lo;  // x - hi.x, y - hi.y, z - hi.z, pot / (2 pi)
+};
+
+__global__ void k_swe_sphere32_pack(View fx, const double* __restrict__ zeta,
+                                    const double* __restrict__ sigma,
+                                    const double* __restrict__ area,
+                                    const int* __restrict__ src2slot, int64_t ns,
+                                    SphSrc32* __restrict__ src, int* __restrict__ slot) {
+  const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = src2slot[k];
+  const double x = fx(j, 0), y = fx(j, 1), z = fx(j, 2);
+  const float xh = float(x), yh = float(y), zh = float(z);
+  const double inv2pi = 1.0 / (2 * kPI);
+  SphSrc32 r;
+  r.hi = make_float4(xh, yh, zh, float(-zeta[j] * area[j] * inv2pi));
+  r.lo = make_float4(float(x - xh), float(y - yh), float(z - zh), float(-sigma[j] * area[j] * inv2pi));
+  src[k] = r;
+  slot[k] = int(j);
+}
+
+template <bool COLL>
+__global__ void __launch_bounds__(kSweNT) k_swe_sphere32(View tx, int64_t nt,
+                                                         const SphSrc32* __restrict__ src,
+                                                         const int* __restrict__ slot, int64_t ns,
+                                                         int64_t chunk_len, float c0,
+                                                         double* __restrict__ part, int64_t tpad) {
+  __shared__ SphSrc32 tile[kSweTile];
+  __shared__ int tslot[COLL ? kSweTile : 1];
+  const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
+  const bool valid = i < nt;
+  float xh[3], xl[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double v = valid ? tx(i, a) : 0.0;
+    xh[a] = float(v);
+    xl[a] = float(v - double(xh[a]));
+  }
+  float S[kSph32NC], C[kSph32NC];
+#pragma unroll
+  for (int k = 0; k < kSph32NC; ++k) S[k] = C[k] = 0.f;
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+    const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += kSweNT) {
+      tile[q] = src[t0 + q];
+      if (COLL) tslot[q] = slot[t0 + q];
+    }
+    __syncthreads();
+    if (!valid) continue;
+    float w[kSph32NC];
+#pragma unroll
+    for (int k = 0; k < kSph32NC; ++k) w[k] = 0.f;
+#pragma unroll 2
+    for (int q = 0; q < m; ++q) {
+      if (COLL && tslot[q] == i) continue;
+      const float4 h = tile[q].hi, l = tile[q].lo;
+      const float d0 = (xh[0] - h.x) + (xl[0] - l.x);
+      const float d1 = (xh[1] - h.y) + (xl[1] - l.y);
+      const float d2 = (xh[2] - h.z) + (xl[2] - l.z);
+      const float dd = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+      const float r = rcp_approx(dd + c0);
+      const float sz = h.w * r, ss = l.w * r;
+      const float R = (sz + sz) * r, Q = (ss + ss) * r;
+      w[0] = fmaf(sz, d0, w[0]);
+      w[1] = fmaf(sz, d1, w[1]);
+      w[2] = fmaf(sz, d2, w[2]);
+      w[3] = fmaf(ss, d0, w[3]);
+      w[4] = fmaf(ss, d1, w[4]);
+      w[5] = fmaf(ss, d2, w[5]);
+      const float r0 = R * d0, r1 = R * d1, r2 = R * d2;
+      const float q0 = Q * d0, q1 = Q * d1, q2 = Q * d2;
+      w[6] += r0;
+      w[7] += r1;
+      w[8] += r2;
+      w[9] += q0;
+      w[10] += q1;
+      w[11] += q2;
+      w[12] = fmaf(r0, d0, w[12]);
+      w[13] = fmaf(r0, d1, w[13]);
+      w[14] = fmaf(r0, d2, w[14]);
+      w[15] = fmaf(r1, d1, w[15]);
+      w[16] = fmaf(r1, d2, w[16]);
+      w[17] = fmaf(r2, d2, w[17]);
+      w[18] = fmaf(q0, d0, w[18]);
+      w[19] = fmaf(q0, d1, w[19]);
+      w[20] = fmaf(q0, d2, w[20]);
+      w[21] = fmaf(q1, d1, w[21]);
+      w[22] = fmaf(q1, d2, w[22]);
+      w[23] = fmaf(q2, d2, w[23]);
+      w[24] += sz;
+      w[25] += ss;
+      w[26] = fmaf(ss, dd, w[26]);
+    }
+#pragma unroll
+    for (int k = 0; k < kSph32NC; ++k) two_sum_acc(S[k], C[k], w[k]);
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int k = 0; k < kSph32NC; ++k) part[(c * kSph32NC + k) * tpad + i] = double(S[k]) + double(C[k]);
+}
+
+__global__ void k_swe_sphere32_out(const double* __restrict__ part, int nchunks, int64_t tpad,
+                                   View tx, int64_t nt, double eps2, View u,
+                                   double* __restrict__ ddot, double* __restrict__ grad,
+                                   int do_velocity) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  double s[kSph32NC];
+#pragma unroll
+  for (int k = 0; k < kSph32NC; ++k) s[k] = 0.0;
+  for (int c = 0; c < nchunks; ++c)
+#pragma unroll
+    for (int k = 0; k < kSph32NC; ++k) s[k] += part[(int64_t(c) * kSph32NC + k) * tpad + i];
+  const double x[3] = {tx(i, 0), tx(i, 1), tx(i, 2)};
+  const double *A = s, *B = s + 3, *U1 = s + 6, *V1 = s + 9;
+  const int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};  // (a, b) -> packed symmetric index
+  const double *U2 = s + 12, *V2 = s + 18;
+  const double Z = s[24], G = s[25], H = s[26];
+  double P[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) P[3 * a + b] = (a == b ? 1.0 : 0.0) - x[a] * x[b];
+  auto cross = [](const double* p, const double* q, double* o) {
+    o[0] = p[1] * q[2] - p[2] * q[1];
+    o[1] = p[2] * q[0] - p[0] * q[2];
+    o[2] = p[0] * q[1] - p[1] * q[0];
+  };
+  if (do_velocity) {
+    double ax[3];
+    cross(A, x, ax);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u(i, a) = ax[a] - (P[3 * a] * B[0] + P[3 * a + 1] * B[1] + P[3 * a + 2] * B[2]);
+  }
+  double u1x[3], pv1[3], zy[3];
+  cross(U1, x, u1x);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    pv1[a] = P[3 * a] * V1[0] + P[3 * a + 1] * V1[1] + P[3 * a + 2] * V1[2];
+    zy[a] = Z * x[a] - A[a];
+  }
+  const double Yx[9] = {0.0, -zy[2], zy[1], zy[2], 0.0, -zy[0], -zy[1], zy[0], 0.0};
+  const double g = G - 0.5 * H;
+  double M[9];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    const double col[3] = {U2[sym[b]], U2[sym[3 + b]], U2[sym[6 + b]]};
+    double t1[3];
+    cross(col, x, t1);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double v2p = V2[sym[3 * a]] * P[b] + V2[sym[3 * a + 1]] * P[3 + b] + V2[sym[3 * a + 2]] * P[6 + b];
+      M[3 * a + b] = eps2 * u1x[a] * x[b] + t1[a] + eps2 * x[a] * pv1[b] + v2p + Yx[3 * a + b] -
+                     g * P[3 * a + b];
+    }
+  }
+  double dsum = 0.0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) dsum = da(dsum, dm(M[3 * a + b], M[3 * b + a]));
+  ddot[i] = dsum;
+  if (grad)
+#pragma unroll
+    for (int k = 0; k < 9; ++k) grad[9 * i + k] = M[k];
+}
+
+void swe_sphere_sums32(lpm_context& ctx, View tx, int64_t nt, View fx, const double* zeta,
+                       const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
+                       double eps, bool collocated, View u, double* ddot, double* grad,
+                       int do_velocity) {
+  if (nt == 0) return;
+  ctx.arena.reset();
+  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
+  const int64_t tpad = nb * kSweNT;
+  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
+  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
+  ctx.arena.reserve(sizeof(int) * (3 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
+                    sizeof(SphSrc32) * size_t(nf) +
+                    sizeof(double) * kSph32NC * size_t(nch_max) * tpad + 8 * 4096);
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
+  SphSrc32* src = static_cast<SphSrc32*>(ctx.arena.take(sizeof(SphSrc32) * std::max<int64_t>(ns, 1)));
+  int* slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(ns, 1)));
+  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
+  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
+  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSph32NC * size_t(nchunks) * tpad));
+  if (ns > 0) {
+    k_swe_sphere32_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(
+        fx, zeta, sigma, area, src2slot, ns, src, slot);
+    ctx.launches++;
+  }
+  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
+  const float c0 = float(2 * eps * eps);
+  if (collocated)
+    k_swe_sphere32<true><<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, slot, ns, chunk_len, c0,
+                                                          part, tpad);
+  else
+    k_swe_sphere32<false><<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, slot, ns, chunk_len, c0,
+                                                           part, tpad);
+  k_swe_sphere32_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(
+      part, nchunks, tpad, tx, nt, eps * eps, u, ddot, grad, do_velocity);
+  ctx.launches += 2;
+  LPM_CUDA(cudaGetLastError());
+}
+
 // Targets tx (nt x 3); sources: face slots fx/zeta/sigma/area/mask (nf);
 // collocated: targets are the face slots themselves (i == j skipped).
 void swe_sphere_sums(lpm_context& ctx, View tx, int64_t nt, View fx, const double* zeta,
                      const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
                      double eps, bool collocated, View u, double* ddot, double* grad,
                      int do_velocity) {
+  if (ctx.precision == LPM_FP32C) {
+    swe_sphere_sums32(ctx, tx, nt, fx, zeta, sigma, area, mask, nf, eps, collocated, u, ddot, grad,
+                      do_velocity);
+    return;
+  }
   if (nt == 0) return;
   ctx.arena.reset();
   const int64_t nb = (nt + kSweNT - 1) / kSweNT;

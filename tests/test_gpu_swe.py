@@ -207,3 +207,37 @@ def test_swe_sphere_views_and_flags(gpu_ctx, oracle):
         check(lib().lpm_swe_sphere_face_sums(gpu_ctx.handle, view(T["fx"]), ptr(o["ddot"]), None,
                                              view(T["fx"]), ptr(T["z"]), ptr(T["s"]), ptr(T["fa"]),
                                              ptr(T["fm"]), fx.shape[0], -1.0, 1))
+
+
+@pytest.mark.parametrize("eps", [0.0, 0.02])
+def test_swe_sphere_fp32c(oracle, eps):
+    """FP32-compensated form (chord moments, hi/lo positions) against the FP64
+    oracle: velocity within 1e-6, gradient tensor and double dot product
+    within 2e-5 (relative to the largest value), leaf targets."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    ctx = core.Context(0, precision=core.FP32C)
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(5)
+    T = _dev(ctx, vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    gv = F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                  want_grad=True)
+    torch.cuda.synchronize()
+    rv = oracle.swe_sphere_sums(vx, fx, zeta, sigma, fa, fm, eps)
+    errs = [_rel(gv["u"].cpu().numpy(), rv[:, :3]), _rel(gv["grad"].cpu().numpy(), rv[:, 3:]),
+            _rel(gv["ddot"].cpu().numpy(), oracle.double_dot(rv[:, 3:]))]
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(4)
+    T = _dev(ctx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    gf = F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                want_grad=True)
+    torch.cuda.synchronize()
+    rf = oracle.swe_sphere_sums(fx, fx, zeta, sigma, fa, fm, eps, collocated=eps == 0)
+    leaf = fm == 0
+    errs += [_rel(gf["u"].cpu().numpy()[leaf], rf[leaf, :3]),
+             _rel(gf["grad"].cpu().numpy()[leaf], rf[leaf, 3:]),
+             _rel(gf["ddot"].cpu().numpy()[leaf], oracle.double_dot(rf[leaf, 3:]))]
+    print("fp32c errors (vertex u, M, ddot; face u, M, ddot):", ["%.2e" % e for e in errs])
+    assert errs[0] < 1e-6 and errs[3] < 1e-6
+    assert max(errs[1], errs[2], errs[4], errs[5]) < 2e-5
