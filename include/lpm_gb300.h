@@ -339,8 +339,10 @@ int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot,
  * double dot product sum_ij M_ij M_ji of the summed gradient tensor
  * M = sum_j grad_kzeta rot_j + grad_ksigma pot_j (rot = -zeta A,
  * pot = -sigma A; sphere_swe_velocity_sums, :335-373).  grad, if not NULL,
- * receives M itself (nv x 9, row-major, contiguous).  FP64; masked faces are
- * skipped. */
+ * receives M itself (nv x 9, row-major, contiguous).  Masked faces are
+ * skipped.  Context precision LPM_FP64 (or LPM_FP64_CHORD): FP64, the
+ * reference's pair arithmetic; LPM_FP32C: FP32 chord-form moments with
+ * compensated sums (velocity ~1e-7, gradient ~1e-5 relative). */
 int lpm_swe_sphere_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot,
                                double* grad, lpm_view vx, int64_t nv,
                                lpm_view fx, const double* fzeta,
