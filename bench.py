@@ -692,6 +692,78 @@ SWE_FLOPS_PER_PAIR = 94
 SWE32_FLOPS_PER_PAIR = 71
 
 
+def swe_plane_measure(ctx, stream, flush, args, lpm_oracle):
+    """Planar SWE sums with PSE (PlanarSWEVertexSums + PlanarSWEFaceSums): quad
+    mesh of [-4, 4]^2 at level --swe-plane-level, a dipole-like vorticity, a
+    smooth divergence and surface, eps = 0.02, pse_eps = h^0.55.  `value` is
+    the FP32C form (--steps timed vertex + face evaluations); the FP64 form is
+    timed once and checked against the oracle on 2,048 vertex targets, and
+    FP32C against FP64 on every vertex."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    level = args.swe_plane_level
+    vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, level, 4.0)
+    zeta = 2 * np.exp(-np.sum((fx - [1.0, 0.0]) ** 2, 1)) - 2 * np.exp(-np.sum((fx + [1.0, 0.0]) ** 2, 1))
+    sigma = 0.3 * np.cos(fx[:, 0]) * np.exp(-np.sum(fx ** 2, 1) / 8)
+    fs = 1 + 0.1 * np.exp(-np.sum(fx ** 2, 1))
+    vs = 1 + 0.1 * np.exp(-np.sum(vx ** 2, 1))
+    eps, pse_eps = 0.02, float(np.sqrt(fa[fm == 0].mean())) ** 0.55
+    dev = torch.device("cuda", torch.cuda.current_device())
+    T = {k: torch.tensor(v, device=dev) for k, v in
+         dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma, fs=fs, vs=vs).items()}
+    ctx.set_precision(core.FP64)
+
+    def step():
+        gv = F.swe_plane_vertex_sums(ctx, T["vx"], T["vs"], T["fx"], T["z"], T["s"], T["fa"],
+                                     T["fm"], T["fs"], eps, pse_eps)
+        F.swe_plane_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], T["fs"], eps,
+                              pse_eps)
+        return gv
+
+    def timed(n):
+        ms, out = 0.0, None
+        for k in range(n):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            out = step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        return ms / n, out
+
+    step()
+    torch.cuda.synchronize()
+    ms, gv = timed(1)
+    ctx.set_precision(core.FP32C)
+    step()
+    ms32, gv32 = timed(max(1, args.steps))
+    ctx.set_precision(core.FP64)
+    nv, ntot, nleaf = vx.shape[0], fx.shape[0], int((fm == 0).sum())
+    idx = np.sort(np.random.default_rng(20261203).choice(nv, min(2048, nv), replace=False))
+    ref = lpm_oracle.swe_plane_sums(vx[idx], vs[idx], fx, zeta, sigma, fa, fm, fs, eps, pse_eps)
+    err, err32 = {}, {}
+    for k, col in (("u", slice(0, 2)), ("du1dx1", 2), ("du1dx2", 3), ("laps", 6), ("psi", 7),
+                   ("phi", 8)):
+        g = gv[k].cpu().numpy()[idx]
+        r = ref[:, col]
+        err[k] = float(np.max(np.abs(g - r)) / np.max(np.abs(r)))
+        g32, g64 = gv32[k].cpu().numpy(), gv[k].cpu().numpy()
+        err32[k] = float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64)))
+    pairs = (nv + ntot) * nleaf
+    return {"value": round(pairs / (ms32 * 1e-3) / 1e9, 3), "unit": UNIT, "dtype": "f32",
+            "ms_per_step": round(ms32, 3),
+            "fp64": {"value": round(pairs / (ms * 1e-3) / 1e9, 4), "ms_per_step": round(ms, 2)},
+            "workload": f"planar SWE vertex + face sums with PSE, quad level {level} on "
+                        f"[-4,4]^2, eps={eps}, pse_eps={pse_eps:.4f}",
+            "interactions_per_step": pairs,
+            "errors_fp32c_vs_fp64_all_vertex_targets": err32,
+            "errors_fp64_vs_oracle_2048_vertex_targets": err}
+
+
 def run_swe(args, device):
     """Spherical shallow-water direct sums (SphereVertexSums + SphereFaceSums,
     src/lpm_swe_kernels.hpp:723-940): icosahedral level --swe-level, every
@@ -811,6 +883,7 @@ def run_swe(args, device):
     ref_d = lpm_oracle.double_dot(ref[:, 3:])
     err64 = {"velocity_linf": float(np.abs(got_u - ref[:, :3]).max() / np.abs(ref[:, :3]).max()),
              "ddot_linf": float(np.abs(got_d - ref_d).max() / np.abs(ref_d).max())}
+    plane = swe_plane_measure(ctx, stream, flush, args, lpm_oracle)
     ach = pairs_per_s * SWE32_FLOPS_PER_PAIR / 1e12
     ach64 = pairs / (ms64 * 1e-3) * SWE_FLOPS_PER_PAIR / 1e12
     return {"metric": "spherical SWE direct sums Ginteractions/s (velocity + double dot)",
@@ -837,6 +910,7 @@ def run_swe(args, device):
                                   "flops_per_pair_credited": SWE_FLOPS_PER_PAIR,
                                   "peak_kind": "measured FP64 FMA peak (lpm_measure_fma_peak)"}},
             "errors_fp32c_vs_fp64_all_leaf_targets": err32,
+            "plane": plane,
             "errors_fp64_vs_oracle_2048_vertex_targets": err64,
             "cpu_baseline": {"value": round(idx.size * nleaf / cpu_s / 1e9, 5), "unit": UNIT,
                              "cores": threads, "kind": "port",
@@ -1027,6 +1101,7 @@ def main():
                          "c5: level 8 on the learned octree far field; "
                          "swe: spherical shallow-water sums (FP64)")
     ap.add_argument("--swe-level", type=int, default=6)
+    ap.add_argument("--swe-plane-level", type=int, default=7)
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
     ap.add_argument("--ff-rho-min", type=float, default=0.25,

@@ -311,8 +311,10 @@ int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops);
  * farea/fmask/fs (nf): velocity u (written if do_velocity), the double dot
  * product du/dx^2 + 2 du/dy dv/dx + dv/dy^2, the four velocity gradients,
  * the PSE surface Laplacian (pse::BivariateOrder8 of width pse_eps), the
- * stream and potential functions.  FP64, the reference's pair arithmetic
- * (planar_swe_sums_rhs_pse, :394-480); masked faces are skipped. */
+ * stream and potential functions; masked faces are skipped.  Context
+ * precision LPM_FP64: the reference's pair arithmetic (planar_swe_sums_rhs_pse,
+ * :394-480); LPM_FP32C: FP32 moment sums with compensation (velocity ~1e-7,
+ * stream/potential ~1e-6, gradients and Laplacian ~1e-5 relative). */
 int lpm_swe_plane_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot,
                               double* du1dx1, double* du1dx2, double* du2dx1,
                               double* du2dx2, double* laps, double* psi,

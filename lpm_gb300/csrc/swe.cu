@@ -154,6 +154,146 @@ __global__ void k_swe_out(const double* __restrict__ part, int nchunks, int64_t 
   o.phi[i] = s[8];
 }
 
+// ---- planar SWE sums, FP32 compensated (context precision LPM_FP32C) ------
+// With d = x - y, R = |d|^2 + eps^2, r = 1/R, a = rot r, b = pot r, every
+// output is a sum of per-pair moments (15 per target):
+//   w0..3 = sum a d0, a d1, b d0, b d1      w4, w5 = sum a, sum b
+//   w6..8 = sum a r (d0^2, d0 d1, d1^2)     w9..11 = the same with b
+//   w12 = sum (s_y - s_x) A lapPSE(|d|^2 / pse_eps^2)
+//   w13, w14 = sum rot lg2 R, sum pot lg2 R
+// and the FP64 epilogue forms u = (-w1 + w2) / 2pi, v = (w0 + w3) / 2pi,
+// du/dx = (w7 - w9) / pi + w5 / 2pi, du/dy = (w8 - w10) / pi - w4 / 2pi,
+// dv/dx = (-w6 - w10) / pi + w4 / 2pi, dv/dy = (-w7 - w11) / pi + w5 / 2pi,
+// lap = w12 / (pi pse_eps^2), psi, phi = -(ln 2 / 4pi) w13, w14.  The PSE
+// kernel uses |d|^2 directly (the reference's sqrt then square is the
+// identity).  Positions and surface heights are split into FP32 hi + lo parts
+// (d and s_y - s_x are small differences of O(1) values).  Three MUFU
+// results (reciprocal, log2, exp2) and ~45 FP32 instructions per pair.
+constexpr int kPl32NC = 15;
+
+struct __align__(16) PlSrc32 {
+  float4 p;  // x hi, y hi, x lo, y lo
+  float4 w;  // rot, pot, area, surface hi
+  float4 e;  // surface lo, slot (int bits), -, -
+};
+
+__global__ void k_swe_plane32_pack(View fx, const double* __restrict__ zeta,
+                                   const double* __restrict__ sigma,
+                                   const double* __restrict__ area, const double* __restrict__ sfc,
+                                   const int* __restrict__ src2slot, int64_t ns,
+                                   PlSrc32* __restrict__ src) {
+  const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (k >= ns) return;
+  const int64_t j = src2slot[k];
+  const double x = fx(j, 0), y = fx(j, 1), sv = sfc[j];
+  const float xh = float(x), yh = float(y), sh = float(sv);
+  PlSrc32 r;
+  r.p = make_float4(xh, yh, float(x - xh), float(y - yh));
+  r.w = make_float4(float(zeta[j] * area[j]), float(sigma[j] * area[j]), float(area[j]), sh);
+  r.e = make_float4(float(sv - sh), __int_as_float(int(j)), 0.f, 0.f);
+  src[k] = r;
+}
+
+template <bool COLL>
+__global__ void __launch_bounds__(kSweNT) k_swe_plane32(View tx, const double* __restrict__ ts,
+                                                        int64_t nt, const PlSrc32* __restrict__ src,
+                                                        int64_t ns, int64_t chunk_len, float e2,
+                                                        float ipse2, double* __restrict__ part,
+                                                        int64_t tpad) {
+  __shared__ PlSrc32 tile[kSweTile];
+  const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
+  const bool valid = i < nt;
+  const double X0 = valid ? tx(i, 0) : 0.0, X1 = valid ? tx(i, 1) : 0.0;
+  const double SX = valid ? ts[i] : 0.0;
+  const float x0h = float(X0), x1h = float(X1), sxh = float(SX);
+  const float x0l = float(X0 - x0h), x1l = float(X1 - x1h), sxl = float(SX - sxh);
+  const float kLog2e = 1.4426950408889634f;
+  float S[kPl32NC], C[kPl32NC];
+#pragma unroll
+  for (int k = 0; k < kPl32NC; ++k) S[k] = C[k] = 0.f;
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+    const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    __syncthreads();
+    for (int q = threadIdx.x; q < m; q += kSweNT) tile[q] = src[t0 + q];
+    __syncthreads();
+    if (!valid) continue;
+    float w[kPl32NC];
+#pragma unroll
+    for (int k = 0; k < kPl32NC; ++k) w[k] = 0.f;
+#pragma unroll 2
+    for (int q = 0; q < m; ++q) {
+      const float4 P = tile[q].p, W = tile[q].w, E = tile[q].e;
+      if (COLL && __float_as_int(E.y) == i) continue;
+      const float d0 = (x0h - P.x) + (x0l - P.z);
+      const float d1 = (x1h - P.y) + (x1l - P.w);
+      const float dd = fmaf(d0, d0, d1 * d1);
+      const float R = dd + e2;
+      const float r = rcp_approx(R);
+      const float L = lg2_approx(R);
+      const float p2 = dd * ipse2;
+      float ex;
+      asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(-p2 * kLog2e));
+      const float poly = fmaf(fmaf(fmaf(-2.f / 3.f, p2, 10.f), p2, -40.f), p2, 40.f);
+      const float ds = (W.w - sxh) + (E.x - sxl);
+      const float a = W.x * r, b = W.y * r;
+      const float a2 = a * r, b2 = b * r;
+      w[0] = fmaf(a, d0, w[0]);
+      w[1] = fmaf(a, d1, w[1]);
+      w[2] = fmaf(b, d0, w[2]);
+      w[3] = fmaf(b, d1, w[3]);
+      w[4] += a;
+      w[5] += b;
+      const float ad0 = a2 * d0, ad1 = a2 * d1, bd0 = b2 * d0, bd1 = b2 * d1;
+      w[6] = fmaf(ad0, d0, w[6]);
+      w[7] = fmaf(ad0, d1, w[7]);
+      w[8] = fmaf(ad1, d1, w[8]);
+      w[9] = fmaf(bd0, d0, w[9]);
+      w[10] = fmaf(bd0, d1, w[10]);
+      w[11] = fmaf(bd1, d1, w[11]);
+      w[12] = fmaf(ds * W.z, poly * ex, w[12]);
+      w[13] = fmaf(W.x, L, w[13]);
+      w[14] = fmaf(W.y, L, w[14]);
+    }
+#pragma unroll
+    for (int k = 0; k < kPl32NC; ++k) two_sum_acc(S[k], C[k], w[k]);
+  }
+  if (!valid) return;
+#pragma unroll
+  for (int k = 0; k < kPl32NC; ++k) part[(c * kPl32NC + k) * tpad + i] = double(S[k]) + double(C[k]);
+}
+
+__global__ void k_swe_plane32_out(const double* __restrict__ part, int nchunks, int64_t tpad,
+                                  int64_t nt, double pse_eps, SweOut o) {
+  const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (i >= nt) return;
+  double w[kPl32NC];
+#pragma unroll
+  for (int k = 0; k < kPl32NC; ++k) w[k] = 0.0;
+  for (int c = 0; c < nchunks; ++c)
+#pragma unroll
+    for (int k = 0; k < kPl32NC; ++k) w[k] += part[(int64_t(c) * kPl32NC + k) * tpad + i];
+  const double ipi = 1.0 / kPI, i2pi = 0.5 / kPI;
+  if (o.do_velocity) {
+    o.u(i, 0) = (w[2] - w[1]) * i2pi;
+    o.u(i, 1) = (w[0] + w[3]) * i2pi;
+  }
+  const double g00 = (w[7] - w[9]) * ipi + w[5] * i2pi;
+  const double g01 = (w[8] - w[10]) * ipi - w[4] * i2pi;
+  const double g10 = -(w[6] + w[10]) * ipi + w[4] * i2pi;
+  const double g11 = -(w[7] + w[11]) * ipi + w[5] * i2pi;
+  o.ddot[i] = da(da(dm(g00, g00), dm(dm(2.0, g01), g10)), dm(g11, g11));
+  o.du1dx1[i] = g00;
+  o.du1dx2[i] = g01;
+  o.du2dx1[i] = g10;
+  o.du2dx2[i] = g11;
+  o.laps[i] = w[12] * ipi / (pse_eps * pse_eps);
+  const double k = -0.6931471805599453 / (4 * kPI);
+  o.psi[i] = k * w[13];
+  o.phi[i] = k * w[14];
+}
+
 // ---- spherical SWE sums ----------------------------------------------------
 // Pair term (sphere_swe_velocity_sums, :335-373) with s = x.y,
 // D = (1 - s) + eps^2, c = x cross y, rot = -zeta A, pot = -sigma A, and
@@ -595,11 +735,55 @@ bool fp_zero(double x) { return std::fabs(x) < 2.220446049250313e-16; }
 
 // Targets tx (nt x 2) with surface ts; sources: face slots fx/zeta/sigma/
 // area/mask/sfc (nf); collocated: targets are the face slots themselves.
+void swe_plane_sums32(lpm_context& ctx, View tx, const double* ts, int64_t nt, View fx,
+                      const double* zeta, const double* sigma, const double* area,
+                      const uint8_t* mask, const double* sfc, int64_t nf, double eps,
+                      double pse_eps, bool collocated, const SweOut& out) {
+  ctx.arena.reset();
+  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
+  const int64_t tpad = nb * kSweNT;
+  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
+  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
+  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
+                    sizeof(PlSrc32) * size_t(nf) +
+                    sizeof(double) * kPl32NC * size_t(nch_max) * tpad + 8 * 4096);
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
+  PlSrc32* src = static_cast<PlSrc32*>(ctx.arena.take(sizeof(PlSrc32) * std::max<int64_t>(ns, 1)));
+  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
+  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
+  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
+  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kPl32NC * size_t(nchunks) * tpad));
+  if (ns > 0) {
+    k_swe_plane32_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
+                                                                            sfc, src2slot, ns, src);
+    ctx.launches++;
+  }
+  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
+  const float e2 = float(eps * eps), ipse2 = float(1.0 / (pse_eps * pse_eps));
+  if (collocated)
+    k_swe_plane32<true><<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, e2, ipse2,
+                                                         part, tpad);
+  else
+    k_swe_plane32<false><<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, e2,
+                                                          ipse2, part, tpad);
+  k_swe_plane32_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, nt,
+                                                                        pse_eps, out);
+  ctx.launches += 2;
+  LPM_CUDA(cudaGetLastError());
+}
+
 void swe_plane_sums(lpm_context& ctx, View tx, const double* ts, int64_t nt, View fx,
                     const double* zeta, const double* sigma, const double* area,
                     const uint8_t* mask, const double* sfc, int64_t nf, double eps,
                     double pse_eps, bool collocated, const SweOut& out) {
   if (nt == 0) return;
+  if (ctx.precision == LPM_FP32C) {
+    swe_plane_sums32(ctx, tx, ts, nt, fx, zeta, sigma, area, mask, sfc, nf, eps, pse_eps,
+                     collocated, out);
+    return;
+  }
   ctx.arena.reset();
   const int64_t nb = (nt + kSweNT - 1) / kSweNT;
   const int64_t tpad = nb * kSweNT;

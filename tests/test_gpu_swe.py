@@ -241,3 +241,44 @@ def test_swe_sphere_fp32c(oracle, eps):
     print("fp32c errors (vertex u, M, ddot; face u, M, ddot):", ["%.2e" % e for e in errs])
     assert errs[0] < 1e-6 and errs[3] < 1e-6
     assert max(errs[1], errs[2], errs[4], errs[5]) < 2e-5
+
+
+@pytest.mark.parametrize("eps", [0.0, 0.05])
+def test_swe_plane_fp32c(oracle, eps):
+    """Planar FP32-compensated form (moments, hi/lo positions and surface)
+    against the FP64 oracle: velocity within 1e-6, stream and potential
+    functions within 3e-6 (the MUFU log2 carries ~2e-7 absolute error per
+    pair), gradients, double dot and PSE Laplacian within 3e-5."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    ctx = core.Context(0, precision=core.FP32C)
+    vx, fx, fa, fm, zeta, sigma, fs, vs = _fields(5)
+    pse_eps = math.sqrt(fa[fm == 0].mean()) ** 0.55
+    d = torch.device("cuda", 0)
+    T = {k: torch.tensor(v, device=d) for k, v in
+         dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, sg=sigma, fs=fs, vs=vs).items()}
+    gv = F.swe_plane_vertex_sums(ctx, T["vx"], T["vs"], T["fx"], T["z"], T["sg"], T["fa"],
+                                 T["fm"], T["fs"], eps, pse_eps)
+    gf = F.swe_plane_face_sums(ctx, T["fx"], T["z"], T["sg"], T["fa"], T["fm"], T["fs"], eps,
+                               pse_eps)
+    torch.cuda.synchronize()
+    rv = oracle.swe_plane_sums(vx, vs, fx, zeta, sigma, fa, fm, fs, eps, pse_eps, collocated=False)
+    rf = oracle.swe_plane_sums(fx, fs, fx, zeta, sigma, fa, fm, fs, eps, pse_eps,
+                               collocated=not eps > 0)
+    tol = {"u": 1e-6, "psi": 3e-6, "phi": 3e-6, "du1dx1": 3e-5, "du1dx2": 3e-5, "du2dx1": 3e-5,
+           "du2dx2": 3e-5, "laps": 3e-5}
+    leaf = fm == 0
+    worst = {}
+    for got, ref, sel in ((gv, rv, slice(None)), (gf, rf, leaf)):
+        cols = {"u": ref[:, 0:2], "du1dx1": ref[:, 2], "du1dx2": ref[:, 3], "du2dx1": ref[:, 4],
+                "du2dx2": ref[:, 5], "laps": ref[:, 6], "psi": ref[:, 7], "phi": ref[:, 8]}
+        for k, t in tol.items():
+            e = _rel(got[k].cpu().numpy()[sel], cols[k][sel])
+            worst[k] = max(worst.get(k, 0.0), e)
+            assert e < t, (k, e)
+        dd = ref[:, 2] ** 2 + 2 * ref[:, 3] * ref[:, 4] + ref[:, 5] ** 2
+        assert _rel(got["ddot"].cpu().numpy()[sel], dd[sel]) < 3e-5
+    print("plane fp32c errors:", {k: "%.1e" % v for k, v in worst.items()})
