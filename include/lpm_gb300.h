@@ -233,6 +233,47 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
                                   const uint8_t* fmask);
 int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches);
 
+/* ---- one-call forms ------------------------------------------------------ */
+/* For hosts that keep no lpm_context: coordinate views with their count, a
+ * precision (LPM_FP64, LPM_FP64_CHORD or LPM_FP32C) and a CUDA stream (NULL =
+ * the legacy default stream).  A context cached per host thread and device
+ * does the work, stream-ordered; switching streams synchronises the previous
+ * one (the cached context's scratch memory is reused by the next call).
+ * want: 1 = velocity, 2 = stream function, 3 = both.  collocated: the
+ * targets are the sources (the same view, n == n_src).
+ * lpm_bve_direct_sum: eps == 0 gives the BVE functors (BVEVertexSolve /
+ * BVEFaceSolve arithmetic, collocated targets skip i == j); eps > 0 the
+ * smoothed sphere kernel of Incompressible2DKernels with the same i == j
+ * rule.  lpm_plane_direct_sum: the planar Incompressible2D sums (collocated
+ * targets skip i == j only when eps is zero, as Incompressible2DActiveSums). */
+typedef struct {
+  const double* p;
+  long long n;
+  long long stride_i;
+  long long stride_c;
+} lpm_crd3;
+int lpm_bve_direct_sum(lpm_crd3 tgt, lpm_crd3 src, const double* zeta,
+                       const double* area, const unsigned char* mask,
+                       long long n_src, int collocated, double eps, int want,
+                       int precision, double* u_out, long long u_stride_i,
+                       long long u_stride_c, double* psi_out,
+                       void* cuda_stream);
+int lpm_plane_direct_sum(lpm_crd3 tgt, lpm_crd3 src, const double* zeta,
+                         const double* area, const unsigned char* mask,
+                         long long n_src, int collocated, double eps, int want,
+                         int precision, double* u_out, long long u_stride_i,
+                         long long u_stride_c, double* psi_out,
+                         void* cuda_stream);
+/* One step of a stepper (the advance_timestep calls above under the step
+ * names), and nsteps RK4 steps of every problem of an ensemble. */
+int lpm_bve_rk4_step(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
+                     lpm_view vvel, lpm_view fx, double* fzeta, lpm_view fvel,
+                     const double* farea, const uint8_t* fmask);
+int lpm_ic2d_rk2_step(lpm_ic2d_rk2* st, lpm_view vx, double* vzeta,
+                      lpm_view vvel, double* vpsi, lpm_view fx, double* fzeta,
+                      lpm_view fvel, double* fpsi, const double* farea,
+                      const uint8_t* fmask);
+
 /* ---- ensembles of independent BVE problems ----------------------------- */
 /* No single reference counterpart: many BVESphere/BVERK4 instances advanced
  * together.  Problem p owns nverts[p] vertex rows and nfaces[p] face-slot
@@ -264,6 +305,9 @@ int lpm_ensemble_nbody_time(lpm_ensemble* e, double* ms, int64_t* launches);
  * autotuning it, e.g. for bitwise-reproducible runs across ensembles.  Call
  * before the first velocity/step call. */
 int lpm_ensemble_set_chunk_len(lpm_ensemble* e, int64_t chunk_len);
+int lpm_ensemble_run(lpm_ensemble* e, int nsteps, lpm_view vx, double* vzeta,
+                     lpm_view vvel, lpm_view fx, double* fzeta, lpm_view fvel,
+                     const double* farea);
 
 /* ---- host-side inputs: meshes and initial conditions -------------------- */
 /* Mesh kinds (restatements of the reference seeds' tree_init,

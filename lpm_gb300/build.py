@@ -20,7 +20,7 @@ OUT = PKG / "_lib"
 LIB = OUT / "liblpm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "ensemble.cu", "farfield.cu",
+CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "oneshot.cu", "ensemble.cu", "farfield.cu",
               "mlp.cu", "ffapi.cu", "mesh_dev.cu", "swe.cu"]
 CXX_SOURCES = ["mesh.cpp", "ics.cpp", "tree.cpp", "vtk.cpp"]
 

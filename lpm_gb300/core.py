@@ -64,7 +64,8 @@ EXPORTS = [
     "lpm_farfield_grad", "lpm_farfield_stats", "lpm_bve_rk4_set_farfield", "lpm_tc_selftest", "lpm_farfield_timing",
     "lpm_octree_stats", "lpm_mesh_build_device", "lpm_swe_plane_vertex_sums",
     "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
-    "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh",
+    "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
+    "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
 ]
 
 
@@ -74,6 +75,12 @@ class LpmError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"lpm error {code}: {msg}")
         self.code = code
+
+
+class Crd3(C.Structure):
+    """lpm_crd3: coordinate view with its count (one-call entry points)."""
+    _fields_ = [("p", C.c_void_p), ("n", C.c_longlong), ("stride_i", C.c_longlong),
+                ("stride_c", C.c_longlong)]
 
 
 class View(C.Structure):
@@ -163,6 +170,13 @@ def _declare(L: C.CDLL) -> None:
         "lpm_swe_sphere_vertex_sums": [vp, V, vp, vp, V, i64, V, vp, vp, vp, vp, i64, dbl, i32],
         "lpm_swe_sphere_face_sums": [vp, V, vp, vp, V, vp, vp, vp, vp, i64, dbl, i32],
         "lpm_mesh_face_vertices": [i32, i32, dbl, C.POINTER(i32), vp],
+        "lpm_bve_direct_sum": [Crd3, Crd3, vp, vp, vp, C.c_longlong, i32, dbl, i32, i32, vp,
+                               C.c_longlong, C.c_longlong, vp, vp],
+        "lpm_plane_direct_sum": [Crd3, Crd3, vp, vp, vp, C.c_longlong, i32, dbl, i32, i32, vp,
+                                 C.c_longlong, C.c_longlong, vp, vp],
+        "lpm_bve_rk4_step": [vp, V, vp, V, V, vp, V, vp, vp],
+        "lpm_ic2d_rk2_step": [vp, V, vp, V, vp, V, vp, V, vp, vp, vp],
+        "lpm_ensemble_run": [vp, i32, V, vp, V, V, vp, V, vp],
         "lpm_vtk_write_polymesh": [C.c_char_p, i32, i64, vp, vp, i64, i32, vp, vp, vp, i32, vp],
     }
     for name, args in sig.items():
@@ -185,6 +199,13 @@ def ptr(t) -> int | None:
     if isinstance(t, np.ndarray):
         return t.ctypes.data
     return t.data_ptr()
+
+
+def crd3(t) -> Crd3:
+    """lpm_crd3 of a 2-D torch tensor (rows = points), any strides."""
+    if t.dim() != 2:
+        raise ValueError("coordinate views must be 2-D (n x ndim)")
+    return Crd3(t.data_ptr(), t.shape[0], t.stride(0), t.stride(1))
 
 
 def view(t) -> View:

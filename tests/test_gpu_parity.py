@@ -250,3 +250,57 @@ def test_tendencies_and_invariants(gpu_ctx, oracle):
     en = F.err_norms(ctx, dev(u + 1e-3), dev(u), dev(fa), dev(fm))
     er = oracle.err_norms(u + 1e-3, u, fa, fm)
     assert np.allclose(en, er, rtol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32C"])
+def test_one_call_direct_sums(gpu_ctx, precision):
+    """lpm_bve_direct_sum / lpm_plane_direct_sum (per-thread context, caller's
+    stream) give the context-based functors' results bit for bit."""
+    import ctypes as C
+
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.core import check, crd3, lib, ptr
+
+    prec = getattr(core, precision)
+    ctx = core.Context(0, precision=prec)
+    d = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=d)
+    for kind, ndim in ((core.MESH_ICOS_TRI, 3), (core.MESH_QUAD_RECT, 2)):
+        vx, fx, fa, fm = core.build_mesh(kind, 4, 1.0)
+        z = np.sin(2 * fx[:, 0]) + fx[:, 1]
+        T = {k: torch.tensor(v, device=d) for k, v in dict(vx=vx, fx=fx, fa=fa, fm=fm, z=z).items()}
+        fn = lib().lpm_bve_direct_sum if ndim == 3 else lib().lpm_plane_direct_sum
+        for eps in (0.0, 0.02):
+            for coll in (0, 1):
+                if ndim == 2 and eps == 0.0 and not coll:
+                    continue
+                tgt = T["fx"] if coll else T["vx"]
+                n = tgt.shape[0]
+                u1 = torch.zeros(n, ndim, dtype=torch.float64, device=d)
+                p1 = torch.zeros(n, dtype=torch.float64, device=d)
+                with torch.cuda.stream(stream):
+                    check(fn(crd3(tgt), crd3(T["fx"]), ptr(T["z"]), ptr(T["fa"]), ptr(T["fm"]),
+                             fx.shape[0], coll, eps, 3, prec, ptr(u1), ndim, 1, ptr(p1),
+                             C.c_void_p(stream.cuda_stream)))
+                stream.synchronize()
+                u2 = torch.zeros_like(u1)
+                p2 = torch.zeros_like(p1)
+                if ndim == 3 and eps == 0.0:
+                    if coll:
+                        F.bve_face_solve(ctx, p2, u2, T["fx"], T["z"], T["fa"], T["fm"])
+                    else:
+                        F.bve_vertex_solve(ctx, p2, u2, T["vx"], T["fx"], T["z"], T["fa"], T["fm"])
+                elif coll:
+                    F.ic2d_active_sums(ctx, u2, p2, T["fx"], T["z"], T["fa"], T["fm"], eps,
+                                       self_rule=1 if ndim == 3 else 0)
+                else:
+                    F.ic2d_passive_sums(ctx, u2, p2, T["vx"], T["fx"], T["z"], T["fa"], T["fm"], eps)
+                torch.cuda.synchronize()
+                # parent slots coincide with a child: non-finite in both
+                for a, b in ((u1, u2), (p1, p2)):
+                    fa_, fb_ = torch.isfinite(a), torch.isfinite(b)
+                    assert torch.equal(fa_, fb_), (kind, eps, coll)
+                    assert torch.equal(a[fa_], b[fb_]), (kind, eps, coll)

@@ -40,6 +40,23 @@ def test_no_gpu_is_reported_cleanly():
     assert e.value.code == core.LPM_ERR_CUDA
 
 
+def test_one_call_argument_checks():
+    """The one-call forms reject bad arguments before touching a device."""
+    L = core.lib()
+    c = core.Crd3(None, 0, 3, 1)
+    for fn in (L.lpm_bve_direct_sum, L.lpm_plane_direct_sum):
+        assert fn(c, c, None, None, None, 0, 0, 0.0, 0, core.FP64, None, 3, 1, None, None) \
+            == core.LPM_ERR_ARG  # want out of range
+        assert fn(c, c, None, None, None, 0, 0, -1.0, 1, core.FP64, None, 3, 1, None, None) \
+            == core.LPM_ERR_ARG  # negative eps
+        d = core.Crd3(None, 5, 3, 1)
+        assert fn(d, c, None, None, None, 0, 1, 0.0, 1, core.FP64, None, 3, 1, None, None) \
+            == core.LPM_ERR_ARG  # collocated with a different target view
+    v = core.View(None, 0, 0)
+    assert L.lpm_ensemble_run(None, -1, v, None, v, v, None, v, None) == core.LPM_ERR_ARG
+    assert L.lpm_ensemble_run(None, 0, v, None, v, v, None, v, None) == core.LPM_OK
+
+
 @pytest.mark.parametrize("kind,level,nv,nf,nleaf", [
     (core.MESH_ICOS_TRI, 4, 2562, 6820, 5120),
     (core.MESH_ICOS_TRI, 7, 163842, 436900, 327680),
