@@ -11,7 +11,9 @@ evaluations over (vertices + leaf faces) x leaf faces.  Inputs are synthetic
 Interactions are counted as in the metric: (Nv + Nf) * Nf per evaluation, Nf =
 leaf faces.  `value` uses the FP32-compensated path with inputs resident in
 HBM; the FP64 path (reference arithmetic) is reported beside it, as are the
-relative errors of the FP32 path against FP64 on the same state.
+relative errors of the FP32 path against FP64 on the same state, and the
+learned form (octree far field + tcgen05 MLP correction, network trained in
+the run) with its error against the same FP64 evaluation.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -314,6 +316,12 @@ def run_ours(args, rank, world, device):
         e_v = rel_errors(base.vu, s64.vu)
         e_f = rel_errors(base.fu, s64.fu, base.fm)
 
+        # ---- the learned far field on the same state (the metric's third
+        # form): network trained here (untimed), then timed velocity
+        # evaluations of the initial state, error vs the FP64 evaluation ----
+        learned = run_learned_eval(args, ctx, stream, base, s64, ipe, device) \
+            if not args.no_learned else None
+
         # ---- accuracy 2: one RK4 step, FP32C vs the same algorithm in FP64
         # (chord form, LPM_FP64_CHORD), same flags; also its throughput ----
         sa, sb = base.clone(), base.clone()
@@ -392,9 +400,89 @@ def run_ours(args, rank, world, device):
                 "one_evaluation_vs_reference_fp64": {"velocity_vertices": e_v,
                                                      "velocity_leaf_faces": e_f},
                 "one_rk4_step_vs_fp64_chord": step_err},
+            "learned": learned,
             "cpu_baseline": cpu,
         }
     return result
+
+
+def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
+    """Octree far field with the learned correction (theta = 0.5, leaves <= 64,
+    order-4 expansion, tcgen05 BF16 MLP for rho >= --ff-rho-min) on the
+    headline workload: RK4 steps of the same state with the far field as the
+    stepper's velocity evaluator (tree topology built once, cell records and
+    lists rebuilt on the device every evaluation), timed like the headline
+    (--warmup, --steps, L2 flushed), and one velocity evaluation of every
+    vertex and leaf face of the initial state compared with the
+    reference-arithmetic FP64 evaluation."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300.farfield import FarField
+
+    theta = 0.4 if args.ff_theta is None else args.ff_theta
+    ff = FarField(theta=theta, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
+    t0 = time.perf_counter()
+    if args.ff_weights:
+        saved = np.load(args.ff_weights)
+        ff.set_weights(saved["w"], saved["norm"])
+        ff.set_network(True)
+    else:
+        ff.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
+                 seed=20261203, level_min=5, level_max=8, eps=EPS)
+    torch.cuda.synchronize(device)
+    train_s = time.perf_counter() - t0
+    leaf = base.fm == 0
+    xall = torch.cat([base.vx, base.fx[leaf]]).contiguous()
+    u64 = torch.cat([s64.vu, s64.fu[leaf]])
+    uall = torch.zeros_like(xall)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    errs = {}
+    for tag, net in (("expansion_only", False), ("learned", True)):
+        ff.set_network(net)
+        ff.velocity(uall, xall, base.fx, base.fz, base.fa, base.fm, EPS)
+        torch.cuda.synchronize(device)
+        nv = base.vx.shape[0]
+        errs[tag] = {"velocity_vertices": rel_errors(uall[:nv], u64[:nv]),
+                     "velocity_leaf_faces": rel_errors(uall[nv:], u64[nv:])}
+    stats = ff.stats()
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+
+    def timed_steps(net):
+        ff.set_network(net)
+        st = base.clone()
+        h = make_stepper(ctx, st, core.FP64_CHORD, flags)
+        core.check(core.lib().lpm_bve_rk4_set_farfield(h, ff.handle, 0))
+        for _ in range(args.warmup):
+            advance(h, st)
+        torch.cuda.synchronize(device)
+        ms = 0.0
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            advance(h, st)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms += a.elapsed_time(b)
+        core.lib().lpm_bve_rk4_destroy(h)
+        return ms / args.steps
+
+    ms_x = timed_steps(False)
+    ms = timed_steps(True)
+    return {"value": round(4 * ipe / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
+            "ms_per_step": round(ms, 3), "theta": theta, "rho_min": args.ff_rho_min,
+            "train_s": round(train_s, 2),
+            "errors_one_evaluation_vs_reference_fp64": errs,
+            "expansion_only": {"value": round(4 * ipe / (ms_x * 1e-3) / 1e9, 3),
+                               "ms_per_step": round(ms_x, 3),
+                               "note": "the same steps without the network (order-4 "
+                                       "expansion on every accepted cell)"},
+            "network_rows_per_evaluation": stats.get("network_rows"),
+            "note": "direct-equivalent interactions per RK4 step with the octree far field "
+                    "and the learned correction as the velocity evaluator (FP64 stage "
+                    "updates); the network is trained in this run on seeded random vortex "
+                    "fields of icosahedral levels 5-8"}
 
 
 def cpu_baseline(host, args):
@@ -961,7 +1049,8 @@ def run_c5(args, device):
     ipe = (nv + nleaf) * nleaf
     st0 = DeviceState((vx, fx, fa, fm, vz, fz), device)
     # ---- network: trained here on the GPU (not in the timed region) ----------
-    ff = FarField(theta=0.5, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
+    theta = 0.5 if args.ff_theta is None else args.ff_theta
+    ff = FarField(theta=theta, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
     t0 = time.perf_counter()
     if args.ff_weights:
         saved = np.load(args.ff_weights)
@@ -1059,7 +1148,7 @@ def run_c5(args, device):
             "dtype": "f32+bf16", "data": "synthetic (generated mesh + Rossby-Haurwitz wave; "
                                           "network trained on seeded random vortex fields)",
             "config": {"workload": f"BVE sphere icosahedral level {L} RK4, RH R=4, eps={EPS}, "
-                                   f"dt={DT}, octree far field theta=0.5 leaf<=64 + learned "
+                                   f"dt={DT}, octree far field theta={theta} leaf<=64 + learned "
                                    f"correction for rho >= {args.ff_rho_min}", "vertices": nv, "leaf_faces": nleaf,
                        "direct_equivalent_interactions_per_step": 4 * ipe,
                        "l2": "flushed between timed steps (512 MiB write)",
@@ -1104,6 +1193,10 @@ def main():
     ap.add_argument("--swe-plane-level", type=int, default=7)
     ap.add_argument("--ff-samples", type=int, default=1 << 24)
     ap.add_argument("--ff-epochs", type=int, default=16)
+    ap.add_argument("--ff-theta", type=float, default=None,
+                    help="far field opening angle (cells accepted when h <= theta (D - r)); "
+                         "default 0.5 for c5 (its specification), 0.4 for the learned "
+                         "block of c2")
     ap.add_argument("--ff-rho-min", type=float, default=0.25,
                     help="c5: learned correction for cells with h/(D - r_block) >= this")
     ap.add_argument("--ff-save", default=None, help="c5: save the trained network (.npz)")
@@ -1113,6 +1206,8 @@ def main():
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--cpu-targets", type=int, default=8192)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="c2: skip the learned far-field evaluation")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the FP32C steps only (for profiler runs)")
     args = ap.parse_args()
