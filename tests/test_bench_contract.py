@@ -1,0 +1,34 @@
+"""The benchmark's reference arm runs on the CPU and prints the one-line JSON
+contract (metric, value, unit, timing keys, the CPU baseline and e2e)."""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_reference_arm_json_line():
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--level",
+                        "3", "--steps", "1", "--warmup", "0", "--cpu-targets", "64"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+              "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference"
+    assert d["value"] > 0 and d["unit"] == "Ginteractions/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_bench_arguments_parse():
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--help"], capture_output=True,
+                       text=True, timeout=120, cwd=ROOT)
+    assert r.returncode == 0
+    for flag in ("--config", "--ff-theta", "--ff-rho-min", "--swe-level", "--no-learned"):
+        assert flag in r.stdout
