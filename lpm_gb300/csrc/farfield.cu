@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(128) k_ff_eval(
     const float4* __restrict__ ys, int64_t nsrc, const float* __restrict__ cd,
     const int4* __restrict__ cells, const int* __restrict__ far, const int* __restrict__ near,
     const int4* __restrict__ cnt, float c0, double* __restrict__ wout, int64_t wstride) {
-  __shared__ float4 buf[kNearBuf];
+  __shared__ __align__(32) float4 buf[kNearBuf];  // read as 32-byte source pairs
   __shared__ float cell[kFarBatch][kCellF];
   __shared__ int4 lf[8];
   const int64_t b = blockIdx.x;
@@ -331,19 +331,50 @@ __global__ void __launch_bounds__(128) k_ff_eval(
       __syncthreads();
       if (t < nl) lf[t] = cells[N[l0 + t]];
       __syncthreads();
+      // sources staged as interleaved pairs (x0 x1 y0 y1 z0 z1 g0 g1) so that
+      // one f32x2 instruction applies two sources to this thread's target
+      float* pb = reinterpret_cast<float*>(buf);
       int o = 0;
       for (int k = 0; k < nl; ++k) {
         const int4 ci = lf[k];
         const int m = min(ci.y, kMaxLeaf);
-        for (int i = t; i < m; i += 128) buf[o + i] = ys[ci.x + i];
+        for (int i = t; i < m; i += 128) {
+          const float4 v = ys[ci.x + i];
+          float* e = pb + 8 * ((o + i) >> 1) + ((o + i) & 1);
+          e[0] = v.x;
+          e[2] = v.y;
+          e[4] = v.z;
+          e[6] = v.w;
+        }
         o += m;
       }
+      if ((o & 1) && t == 0) {  // odd count: a zero-strength partner at the origin
+        float* e = pb + 8 * (o >> 1) + 1;
+        e[0] = e[2] = e[4] = e[6] = 0.f;
+      }
       __syncthreads();
-      float w0 = 0.f, w1 = 0.f, w2 = 0.f;
-      for (int i = 0; i < o; ++i) chord_acc(x.x, x.y, x.z, buf[i], c0, w0, w1, w2);
-      two_sum_acc(S0, C0, w0);
-      two_sum_acc(S1, C1, w1);
-      two_sum_acc(S2, C2, w2);
+      const u64 X2 = pk2(x.x, x.x), Y2 = pk2(x.y, x.y), Z2 = pk2(x.z, x.z), C02 = pk2(c0, c0);
+      u64 W0 = 0ull, W1 = 0ull, W2 = 0ull;
+      const ulonglong4* pr = reinterpret_cast<const ulonglong4*>(buf);
+#pragma unroll 4
+      for (int i = 0; i < (o + 1) >> 1; ++i) {
+        const ulonglong4 s = pr[i];  // (x0 x1) (y0 y1) (z0 z1) (g0 g1)
+        const u64 dx = sub2(X2, s.x), dy = sub2(Y2, s.y), dz = sub2(Z2, s.z);
+        const u64 q = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, C02)));
+        float qa, qb;
+        upk2(q, qa, qb);
+        const u64 w = mul2(s.w, pk2(rcp_approx(qa), rcp_approx(qb)));
+        W0 = fma2(w, dx, W0);
+        W1 = fma2(w, dy, W1);
+        W2 = fma2(w, dz, W2);
+      }
+      float a0, b0, a1, b1, a2, b2;
+      upk2(W0, a0, b0);
+      upk2(W1, a1, b1);
+      upk2(W2, a2, b2);
+      two_sum_acc(S0, C0, a0 + b0);
+      two_sum_acc(S1, C1, a1 + b1);
+      two_sum_acc(S2, C2, a2 + b2);
       // leaves larger than kMaxLeaf (coincident points at the deepest level)
       for (int k = 0; k < nl; ++k) {
         const int4 ci = lf[k];
