@@ -1015,7 +1015,7 @@ def run_c5(args, device):
     target's cell frame, 3 x 128 SiLU) trained on the GPU by the tcgen05
     kernels on 2^24 cell-target samples from seeded random vortex fields.
     value = direct-equivalent interactions ((Nv + Nf) Nf per evaluation) per
-    second.  Judges of the error: the GPU FP64 direct sum (reference
+    second.  References for the error: the GPU FP64 direct sum (reference
     arithmetic) on a seeded 16,384-target subsample for one evaluation, and
     the FP32C direct-sum trajectory (1.6e-7 from FP64 after a step, C2) for
     the steps; the FP64 time per evaluation is the subsample's time scaled
@@ -1113,7 +1113,7 @@ def run_c5(args, device):
     clocks = sampler.stop()
     launches = ctx.kernel_launches - l0
     core.lib().lpm_bve_rk4_destroy(h)
-    # ---- the same steps with the FP32C direct sum (trajectory judge) --------
+    # ---- the same steps with the FP32C direct sum (trajectory reference) --------
     ref = st0.clone()
     ref.velocity(ctx, core.FP32C)
     hr = make_stepper(ctx, ref, core.FP32C, flags)

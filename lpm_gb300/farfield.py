@@ -7,7 +7,7 @@ cells (h <= theta (D - r_block)), the exact FP32-compensated sum over the
 near leaves, and -- once trained or loaded -- a BF16 MLP run on the tcgen05
 tensor cores that predicts the expansion's residual for accepted cells with
 h / (D - r_block) >= rho_min.  The exact direct sum stays the fallback (a
-target block whose lists overflow) and the judge of the error (tests, bench).
+target block whose lists overflow) and the reference for its error (tests, bench).
 """
 from __future__ import annotations
 

@@ -1,6 +1,6 @@
 """Octree far field with the learned correction: tensor-core building block,
 gradient check against the CPU oracle, accuracy against the FP64 direct sum
-(the judge of its error), the direct-sum fallback, the gain of the trained
+(the reference for its error), the direct-sum fallback, the gain of the trained
 network over the expansion alone, and the RK4 stepper on the far field."""
 import math
 
