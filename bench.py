@@ -1112,6 +1112,31 @@ def run_c5(args, device):
         ms += a.elapsed_time(b)
     clocks = sampler.stop()
     launches = ctx.kernel_launches - l0
+    # ---- e2e: the state in host buffers, copied in and out inside the timing
+    # (the device state is restored afterwards for the trajectory comparison)
+    names = ("vx", "vz", "vu", "fx", "fz", "fu")
+    keep = {k: getattr(st, k).clone() for k in names}
+    hostbufs = {k: getattr(st, k).cpu().pin_memory() for k in names}
+    h2d = sum(t.numel() * t.element_size() for t in hostbufs.values())
+    ms_e2e = 0.0
+    n_e2e = max(1, args.steps // 2)
+    for k in range(n_e2e):
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for name, hb in hostbufs.items():
+            getattr(st, name).copy_(hb, non_blocking=True)
+        advance(h, st)
+        for name, hb in hostbufs.items():
+            hb.copy_(getattr(st, name), non_blocking=True)
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        ms_e2e += a.elapsed_time(b)
+    e2e = {"value": round(4 * ipe * n_e2e / (ms_e2e * 1e-3) / 1e9, 3), "unit": UNIT,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d}
+    for k in names:
+        getattr(st, k).copy_(keep[k])
+    torch.cuda.synchronize(device)
     core.lib().lpm_bve_rk4_destroy(h)
     # ---- the same steps with the FP32C direct sum (trajectory reference) --------
     ref = st0.clone()
@@ -1157,6 +1182,7 @@ def run_c5(args, device):
                                      "batch": 16384, "seconds": round(train_s, 2),
                                      "loss_per_epoch": [round(float(x), 6) for x in loss]})},
             "mesh_build_seconds": {"host": round(mesh_host_s, 3), "device": round(mesh_dev_s, 4)},
+            "e2e": e2e,
             "speedup_vs_gpu_fp64_direct": round(fp64_eval_s / (step_s / 4), 1),
             "fp64_direct": {"seconds_per_evaluation": round(fp64_eval_s, 3),
                             "value": round(ipe / fp64_eval_s / 1e9, 3),
