@@ -92,3 +92,53 @@ def test_two_rank_sharding_matches_single_rank(tmp_path, oracle):
     assert sorted(sum(problem_assignment([1, 5, 3, 2, 2], 2), [])) == [0, 1, 2, 3, 4]
     # balanced slices cover all targets
     assert sum(target_slice(10, 3, r).stop - target_slice(10, 3, r).start for r in range(3)) == 10
+
+
+def _swe_worker(rank, world, port, out_dir):
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import torch
+    import torch.distributed as dist
+
+    import lpm_oracle
+    from lpm_gb300 import core
+    from lpm_gb300.partition import target_slice
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    lpm_oracle.set_threads(1)
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    zeta = np.sin(2 * fx[:, 0]) + fx[:, 2]
+    sigma = np.cos(3 * fx[:, 1])
+    sl = target_slice(vx.shape[0], world, rank)
+    out = lpm_oracle.swe_sphere_sums(vx[sl], fx, zeta, sigma, fa, fm, 0.02)
+    n = [target_slice(vx.shape[0], world, r).stop - target_slice(vx.shape[0], world, r).start
+         for r in range(world)]
+    mine = torch.zeros(max(n), 12, dtype=torch.float64)
+    mine[: out.shape[0]] = torch.from_numpy(out)
+    parts = [torch.zeros_like(mine) for _ in range(world)]
+    dist.all_gather(parts, mine)
+    if rank == 0:
+        full = torch.cat([parts[r][: n[r]] for r in range(world)])
+        np.save(os.path.join(out_dir, "swe_sharded.npy"), full.numpy())
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.timeout(300)
+def test_two_rank_swe_sharding_matches_single_rank(tmp_path, oracle):
+    """The spherical SWE sums shard by targets the same way: no exchange but
+    the final gather, identical bits."""
+    import torch.multiprocessing as mp
+
+    from lpm_gb300 import core
+
+    port = _free_port()
+    mp.start_processes(_swe_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True,
+                       start_method="spawn")
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    zeta = np.sin(2 * fx[:, 0]) + fx[:, 2]
+    sigma = np.cos(3 * fx[:, 1])
+    ref = oracle.swe_sphere_sums(vx, fx, zeta, sigma, fa, fm, 0.02)
+    assert np.array_equal(np.load(tmp_path / "swe_sharded.npy"), ref)
