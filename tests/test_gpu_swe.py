@@ -162,7 +162,8 @@ def test_swe_sphere_parity(gpu_ctx, oracle, eps):
     assert _rel(gf["ddot"].cpu().numpy()[leaf], oracle.double_dot(rf[leaf, 3:])) < 1e-12
 
 
-def test_swe_sphere_views_and_flags(gpu_ctx, oracle):
+@pytest.mark.parametrize("precision", ["FP64", "FP32C"])
+def test_swe_sphere_views_and_flags(oracle, precision):
     """LayoutLeft-style strided views, do_velocity = 0 keeps u, no grad
     pointer, all sources masked, zero targets, argument errors."""
     import torch
@@ -171,6 +172,7 @@ def test_swe_sphere_views_and_flags(gpu_ctx, oracle):
     from lpm_gb300 import functors as F
     from lpm_gb300.core import check, lib, ptr, view
 
+    gpu_ctx = core.Context(0, precision=getattr(core, precision))
     vx, fx, fa, fm, zeta, sigma = _sphere_fields(3)
     T = _dev(gpu_ctx, vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
     ref = F.swe_sphere_vertex_sums(gpu_ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"],
@@ -282,3 +284,34 @@ def test_swe_plane_fp32c(oracle, eps):
         dd = ref[:, 2] ** 2 + 2 * ref[:, 3] * ref[:, 4] + ref[:, 5] ** 2
         assert _rel(got["ddot"].cpu().numpy()[sel], dd[sel]) < 3e-5
     print("plane fp32c errors:", {k: "%.1e" % v for k, v in worst.items()})
+
+
+def test_swe_plane_fp32c_views_and_flags():
+    """Planar FP32C form: LayoutLeft-style views give the same bits as AoS,
+    do_velocity = 0 keeps u, all sources masked give zeros."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    ctx = core.Context(0, precision=core.FP32C)
+    vx, fx, fa, fm, zeta, sigma, fs, vs = _fields(3)
+    d = torch.device("cuda", 0)
+    T = {k: torch.tensor(v, device=d) for k, v in
+         dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, sg=sigma, fs=fs, vs=vs).items()}
+    ref = F.swe_plane_vertex_sums(ctx, T["vx"], T["vs"], T["fx"], T["z"], T["sg"], T["fa"],
+                                  T["fm"], T["fs"], 0.05, 0.3)
+
+    def soa(a, extra=7):
+        buf = torch.zeros(a.shape[1], a.shape[0] + extra, dtype=torch.float64, device=a.device)
+        buf[:, :a.shape[0]] = a.T
+        return buf[:, :a.shape[0]].T
+    got = F.swe_plane_vertex_sums(ctx, soa(T["vx"]), T["vs"], soa(T["fx"]), T["z"], T["sg"],
+                                  T["fa"], T["fm"], T["fs"], 0.05, 0.3)
+    torch.cuda.synchronize()
+    for k in ("u", "ddot", "laps", "psi", "phi"):
+        assert torch.equal(got[k], ref[k]), k
+    z = F.swe_plane_face_sums(ctx, T["fx"], T["z"], T["sg"], T["fa"], torch.ones_like(T["fm"]),
+                              T["fs"], 0.05, 0.3)
+    torch.cuda.synchronize()
+    assert not bool(z["u"].any()) and not bool(z["psi"].any())
