@@ -645,43 +645,66 @@ __global__ void k_swe_sphere32_out(const double* __restrict__ part, int nchunks,
     for (int k = 0; k < 9; ++k) grad[9 * i + k] = M[k];
 }
 
+// Scratch and chunking shared by the four SWE paths: 128 targets per CTA,
+// sources compacted (masked slots dropped) and split into chunks of whole
+// 256-source tiles, about four waves of CTAs; ncomp FP64 partials per
+// (chunk, target), added in fixed order by the epilogue.
+struct SwePlan {
+  int64_t nb = 0, tpad = 0, ns = 0, chunk_len = 0;
+  int nchunks = 1;
+  int* src2slot = nullptr;
+  void* src = nullptr;     // ns packed source records
+  int* slot = nullptr;     // ns slot indices (when asked for)
+  double* part = nullptr;  // [chunk][ncomp][tpad]
+  dim3 grid() const { return dim3{unsigned(nb), unsigned(nchunks), 1u}; }
+};
+
+SwePlan swe_plan(lpm_context& ctx, const uint8_t* mask, int64_t nt, int64_t nf, size_t rec_bytes,
+                 int ncomp, bool want_slot) {
+  SwePlan p;
+  ctx.arena.reset();
+  p.nb = (nt + kSweNT - 1) / kSweNT;
+  p.tpad = p.nb * kSweNT;
+  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + p.nb - 1) / p.nb);
+  const int64_t nch_max =
+      std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
+  ctx.arena.reserve(sizeof(int) * (3 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
+                    rec_bytes * size_t(nf) + sizeof(double) * ncomp * size_t(nch_max) * p.tpad +
+                    8 * 4096);
+  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  p.src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
+  p.ns = compact_sources(ctx, mask, nf, slot2src, p.src2slot);
+  p.src = ctx.arena.take(rec_bytes * std::max<int64_t>(p.ns, 1));
+  if (want_slot) p.slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(p.ns, 1)));
+  int64_t len = (p.ns + nch_max - 1) / nch_max;
+  p.chunk_len = std::max<int64_t>(kSweTile, (len + kSweTile - 1) / kSweTile * kSweTile);
+  p.nchunks = int(std::max<int64_t>(1, (p.ns + p.chunk_len - 1) / p.chunk_len));
+  p.part = static_cast<double*>(ctx.arena.take(sizeof(double) * ncomp * size_t(p.nchunks) * p.tpad));
+  return p;
+}
+
+unsigned blocks256(int64_t n) { return unsigned((n + 255) / 256); }
+
 void swe_sphere_sums32(lpm_context& ctx, View tx, int64_t nt, View fx, const double* zeta,
                        const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
                        double eps, bool collocated, View u, double* ddot, double* grad,
                        int do_velocity) {
-  if (nt == 0) return;
-  ctx.arena.reset();
-  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
-  const int64_t tpad = nb * kSweNT;
-  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
-  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
-  ctx.arena.reserve(sizeof(int) * (3 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
-                    sizeof(SphSrc32) * size_t(nf) +
-                    sizeof(double) * kSph32NC * size_t(nch_max) * tpad + 8 * 4096);
-  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
-  SphSrc32* src = static_cast<SphSrc32*>(ctx.arena.take(sizeof(SphSrc32) * std::max<int64_t>(ns, 1)));
-  int* slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(ns, 1)));
-  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
-  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
-  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
-  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSph32NC * size_t(nchunks) * tpad));
-  if (ns > 0) {
-    k_swe_sphere32_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(
-        fx, zeta, sigma, area, src2slot, ns, src, slot);
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(SphSrc32), kSph32NC, true);
+  auto* src = static_cast<SphSrc32*>(p.src);
+  if (p.ns > 0) {
+    k_swe_sphere32_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
+                                                                 p.src2slot, p.ns, src, p.slot);
     ctx.launches++;
   }
-  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
   const float c0 = float(2 * eps * eps);
   if (collocated)
-    k_swe_sphere32<true><<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, slot, ns, chunk_len, c0,
-                                                          part, tpad);
+    k_swe_sphere32<true><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, p.slot, p.ns,
+                                                              p.chunk_len, c0, p.part, p.tpad);
   else
-    k_swe_sphere32<false><<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, slot, ns, chunk_len, c0,
-                                                           part, tpad);
-  k_swe_sphere32_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(
-      part, nchunks, tpad, tx, nt, eps * eps, u, ddot, grad, do_velocity);
+    k_swe_sphere32<false><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, p.slot, p.ns,
+                                                               p.chunk_len, c0, p.part, p.tpad);
+  k_swe_sphere32_out<<<blocks256(nt), 256, 0, ctx.stream>>>(p.part, p.nchunks, p.tpad, tx, nt,
+                                                            eps * eps, u, ddot, grad, do_velocity);
   ctx.launches += 2;
   LPM_CUDA(cudaGetLastError());
 }
@@ -692,38 +715,23 @@ void swe_sphere_sums(lpm_context& ctx, View tx, int64_t nt, View fx, const doubl
                      const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
                      double eps, bool collocated, View u, double* ddot, double* grad,
                      int do_velocity) {
+  if (nt == 0) return;
   if (ctx.precision == LPM_FP32C) {
     swe_sphere_sums32(ctx, tx, nt, fx, zeta, sigma, area, mask, nf, eps, collocated, u, ddot, grad,
                       do_velocity);
     return;
   }
-  if (nt == 0) return;
-  ctx.arena.reset();
-  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
-  const int64_t tpad = nb * kSweNT;
-  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
-  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
-  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
-                    sizeof(SphSrc) * size_t(nf) + sizeof(double) * kSphNC * size_t(nch_max) * tpad +
-                    8 * 4096);
-  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
-  SphSrc* src = static_cast<SphSrc*>(ctx.arena.take(sizeof(SphSrc) * std::max<int64_t>(ns, 1)));
-  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
-  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
-  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
-  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSphNC * size_t(nchunks) * tpad));
-  if (ns > 0) {
-    k_swe_sphere_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
-                                                                           src2slot, ns, src);
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(SphSrc), kSphNC, false);
+  auto* src = static_cast<SphSrc*>(p.src);
+  if (p.ns > 0) {
+    k_swe_sphere_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, p.src2slot,
+                                                               p.ns, src);
     ctx.launches++;
   }
-  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
-  k_swe_sphere<<<grid, kSweNT, 0, ctx.stream>>>(tx, nt, src, ns, chunk_len, eps,
-                                                collocated ? 1 : 0, part, tpad);
-  k_swe_sphere_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, tx, nt,
-                                                                       u, ddot, grad, do_velocity);
+  k_swe_sphere<<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, p.ns, p.chunk_len, eps,
+                                                    collocated ? 1 : 0, p.part, p.tpad);
+  k_swe_sphere_out<<<blocks256(nt), 256, 0, ctx.stream>>>(p.part, p.nchunks, p.tpad, tx, nt, u,
+                                                          ddot, grad, do_velocity);
   ctx.launches += 2;
   LPM_CUDA(cudaGetLastError());
 }
@@ -739,37 +747,22 @@ void swe_plane_sums32(lpm_context& ctx, View tx, const double* ts, int64_t nt, V
                       const double* zeta, const double* sigma, const double* area,
                       const uint8_t* mask, const double* sfc, int64_t nf, double eps,
                       double pse_eps, bool collocated, const SweOut& out) {
-  ctx.arena.reset();
-  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
-  const int64_t tpad = nb * kSweNT;
-  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
-  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
-  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
-                    sizeof(PlSrc32) * size_t(nf) +
-                    sizeof(double) * kPl32NC * size_t(nch_max) * tpad + 8 * 4096);
-  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
-  PlSrc32* src = static_cast<PlSrc32*>(ctx.arena.take(sizeof(PlSrc32) * std::max<int64_t>(ns, 1)));
-  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
-  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
-  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
-  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kPl32NC * size_t(nchunks) * tpad));
-  if (ns > 0) {
-    k_swe_plane32_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
-                                                                            sfc, src2slot, ns, src);
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(PlSrc32), kPl32NC, false);
+  auto* src = static_cast<PlSrc32*>(p.src);
+  if (p.ns > 0) {
+    k_swe_plane32_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, sfc,
+                                                                p.src2slot, p.ns, src);
     ctx.launches++;
   }
-  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
   const float e2 = float(eps * eps), ipse2 = float(1.0 / (pse_eps * pse_eps));
   if (collocated)
-    k_swe_plane32<true><<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, e2, ipse2,
-                                                         part, tpad);
+    k_swe_plane32<true><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, p.ns, p.chunk_len,
+                                                             e2, ipse2, p.part, p.tpad);
   else
-    k_swe_plane32<false><<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, e2,
-                                                          ipse2, part, tpad);
-  k_swe_plane32_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, nt,
-                                                                        pse_eps, out);
+    k_swe_plane32<false><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, p.ns, p.chunk_len,
+                                                              e2, ipse2, p.part, p.tpad);
+  k_swe_plane32_out<<<blocks256(nt), 256, 0, ctx.stream>>>(p.part, p.nchunks, p.tpad, nt, pse_eps,
+                                                           out);
   ctx.launches += 2;
   LPM_CUDA(cudaGetLastError());
 }
@@ -784,32 +777,16 @@ void swe_plane_sums(lpm_context& ctx, View tx, const double* ts, int64_t nt, Vie
                      collocated, out);
     return;
   }
-  ctx.arena.reset();
-  const int64_t nb = (nt + kSweNT - 1) / kSweNT;
-  const int64_t tpad = nb * kSweNT;
-  // chunks: about 4 waves of CTAs
-  const int64_t want = std::max<int64_t>(1, (int64_t(ctx.num_sms) * 4 * 8 + nb - 1) / nb);
-  const int64_t nch_max = std::max<int64_t>(1, std::min<int64_t>(want, (nf + kSweTile - 1) / kSweTile));
-  ctx.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
-                    sizeof(SweSrc) * size_t(nf) + sizeof(double) * kSweNC * size_t(nch_max) * tpad +
-                    8 * 4096);
-  int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  int* src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
-  const int64_t ns = compact_sources(ctx, mask, nf, slot2src, src2slot);
-  SweSrc* src = static_cast<SweSrc*>(ctx.arena.take(sizeof(SweSrc) * std::max<int64_t>(ns, 1)));
-  int64_t chunk_len = (ns + nch_max - 1) / std::max<int64_t>(nch_max, 1);
-  chunk_len = std::max<int64_t>(kSweTile, (chunk_len + kSweTile - 1) / kSweTile * kSweTile);
-  const int nchunks = int(std::max<int64_t>(1, (ns + chunk_len - 1) / chunk_len));
-  double* part = static_cast<double*>(ctx.arena.take(sizeof(double) * kSweNC * size_t(nchunks) * tpad));
-  if (ns > 0) {
-    k_swe_pack<<<unsigned((ns + 255) / 256), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, sfc,
-                                                                    src2slot, ns, src);
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(SweSrc), kSweNC, false);
+  auto* src = static_cast<SweSrc*>(p.src);
+  if (p.ns > 0) {
+    k_swe_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, sfc, p.src2slot,
+                                                        p.ns, src);
     ctx.launches++;
   }
-  const dim3 grid{unsigned(nb), unsigned(nchunks), 1u};
-  k_swe_plane<<<grid, kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, ns, chunk_len, eps, pse_eps,
-                                               collocated ? 1 : 0, part, tpad);
-  k_swe_out<<<unsigned((nt + 255) / 256), 256, 0, ctx.stream>>>(part, nchunks, tpad, nt, out);
+  k_swe_plane<<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, ts, nt, src, p.ns, p.chunk_len, eps, pse_eps,
+                                                   collocated ? 1 : 0, p.part, p.tpad);
+  k_swe_out<<<blocks256(nt), 256, 0, ctx.stream>>>(p.part, p.nchunks, p.tpad, nt, out);
   ctx.launches += 2;
   LPM_CUDA(cudaGetLastError());
 }
