@@ -118,7 +118,7 @@ __global__ void k_pack_src(const int* src2slot, int64_t nsrc, int64_t npad,
         make_src_f32(__double2float_rn(p0), __double2float_rn(p1),
                      __double2float_rn(p2), __double2float_rn(g));
   } else {
-    reinterpret_cast<double4*>(out)[k] = make_double4(p0, p1, p2, g);
+    reinterpret_cast<double4_16a*>(out)[k] = make_double4_16a(p0, p1, p2, g);
   }
 }
 
@@ -141,9 +141,9 @@ __global__ void k_pack_tgt(int64_t off, int64_t n, View x, int ndim,
         make_float4(__double2float_rn(p0), __double2float_rn(p1),
                     __double2float_rn(p2), __double2float_rn(gs));
   } else if (MODE == M_C64) {
-    reinterpret_cast<double4*>(out)[off + i] = make_double4(p0, p1, p2, gs);
+    reinterpret_cast<double4_16a*>(out)[off + i] = make_double4_16a(p0, p1, p2, gs);
   } else {
-    reinterpret_cast<double4*>(out)[off + i] = make_double4(p0, p1, p2, 0.0);
+    reinterpret_cast<double4_16a*>(out)[off + i] = make_double4_16a(p0, p1, p2, 0.0);
     tself[off + i] = self;
   }
 }
@@ -155,7 +155,7 @@ __global__ void k_fill_pad_tgt(int64_t from, int64_t to, bool f32, void* out,
   if (f32) {
     reinterpret_cast<float4*>(out)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   } else {
-    reinterpret_cast<double4*>(out)[i] = make_double4(0, 0, 0, 0);
+    reinterpret_cast<double4_16a*>(out)[i] = make_double4_16a(0, 0, 0, 0);
     tself[i] = -1;
   }
 }
@@ -167,7 +167,7 @@ __global__ void k_sum_g_partial(const void* src, bool f32, int64_t n, double* pa
   for (int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * 256)
     s += f32 ? (double)static_cast<const SrcF32*>(src)[k].b.z
-             : static_cast<const double4*>(src)[k].w;
+             : static_cast<const double4_16a*>(src)[k].w;
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
@@ -212,7 +212,7 @@ __global__ void k_combine(const double* __restrict__ part, int nchunks,
   double pos[3] = {x(i, 0), x(i, 1), NDIM == 3 ? x(i, 2) : 0.0};
   double uu[3], ps = 0;
   const double gs = MODE == M_C32 ? (double)static_cast<const float4*>(tgt)[t].w
-                                  : static_cast<const double4*>(tgt)[t].w;
+                                  : static_cast<const double4_16a*>(tgt)[t].w;
   chord_epilogue<MODE, NDIM, WU, WP>(a, pos, gs, sg, c0, uu, &ps);
   if (WU)
 #pragma unroll
@@ -297,7 +297,7 @@ void launch_f64(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
                 const int* tself, const void* src, double* part, double eps2) {
   dim3 grid(unsigned(p.ntgt_pad / (F64_NT * F64_R)), unsigned(p.nchunks));
   nbody_f64<FORM, WU, WP, F64_R, F64_NT, F64_TILE><<<grid, F64_NT, 0, ctx.stream>>>(
-      static_cast<const double4*>(tgt), tself, static_cast<const double4*>(src),
+      static_cast<const double4_16a*>(tgt), tself, static_cast<const double4_16a*>(src),
       p.ntgt_pad, p.nsrc_pad, p.chunk_len, eps2, part, ctx.d_err);
   ctx.launches++;
 }
@@ -552,8 +552,8 @@ void direct_sum(lpm_context& ctx, const SumSpec& spec, const SrcSpec& src,
   // Upper bounds first, so one reservation covers the whole call.
   NbodyPlan p = plan_nbody(ctx, spec.precision, ndim, spec.form, spec.want_u,
                            spec.want_psi, ntgt, src.nslots);
-  const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4);  // target record
-  const size_t srec = 32;  // source record: SrcF32 or double4
+  const size_t rec = m == M_C32 ? sizeof(float4) : sizeof(double4_16a);  // target record
+  const size_t srec = 32;  // source record: SrcF32 or double4_16a
   const size_t need = 4096 + sizeof(int) * (2 * size_t(src.nslots) + 2 * (size_t(src.nslots) / SCAN_BLOCK + 2)) +
                       srec * size_t(p.nsrc_pad) + rec * size_t(p.ntgt_pad) +
                       sizeof(int) * size_t(p.ntgt_pad) + p.part_bytes_max() +

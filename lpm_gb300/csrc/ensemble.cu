@@ -217,7 +217,7 @@ struct lpm_ensemble {
     d_spad = static_cast<int64_t*>(upload(spad));
     const size_t rec = f32() ? 16 : 32;
     tgt = dalloc(rec * T);
-    src = dalloc(32 * S);  // SrcF32 / double4
+    src = dalloc(32 * S);  // SrcF32 / double4_16a
     LPM_CUDA(cudaMemset(tgt, 0, rec * T));
     LPM_CUDA(cudaMemset(src, 0, 32 * S));
     counter = static_cast<int*>(dalloc(sizeof(int)));
@@ -328,8 +328,8 @@ struct lpm_ensemble {
     else
       lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE>
           <<<grid, lpm::F64_NT, 0, c.stream>>>(
-              items, int(nitems), counter, static_cast<const double4*>(tgt),
-              static_cast<const double4*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
+              items, int(nitems), counter, static_cast<const double4_16a*>(tgt),
+              static_cast<const double4_16a*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
               chunk_len, c0(), part, c.d_err);
     c.launches++;
     if (timed) {

@@ -1,7 +1,7 @@
 // farfield.cu -- octree evaluation of the BVE sphere velocity sum.
 //
 // Per evaluation (all on the context stream, capturable in a CUDA graph):
-//   k_ff_sort_src   packed double4 sources -> Morton-ordered float4
+//   k_ff_sort_src   packed double4_16a sources -> Morton-ordered float4
 //   k_ff_cells      per cell: centre, radius, frame, moments to order 4
 //                   (FP32 per 32-point batch, FP64 across batches and threads)
 //   k_ff_tblocks    per block of 128 Morton-ordered targets: centre, radius
@@ -34,11 +34,11 @@ namespace {
 
 __constant__ ff::CplxTable kCplx = ff::make_cplx_table();
 
-__global__ void k_ff_sort_src(const double4* __restrict__ src, const int* __restrict__ perm,
+__global__ void k_ff_sort_src(const double4_16a* __restrict__ src, const int* __restrict__ perm,
                               int64_t n, float4* __restrict__ ys) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (k >= n) return;
-  const double4 s = src[perm[k]];
+  const double4_16a s = src[perm[k]];
   ys[k] = make_float4(float(s.x), float(s.y), float(s.z), float(s.w));
 }
 
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(128) k_ff_cells(const float4* __restrict__ ys,
 
 // One CTA (128 threads) per target block: Morton-ordered FP32 positions and
 // the block's bounding sphere.
-__global__ void __launch_bounds__(128) k_ff_tblocks(const double4* __restrict__ tgt,
+__global__ void __launch_bounds__(128) k_ff_tblocks(const double4_16a* __restrict__ tgt,
                                                     const int* __restrict__ tslot,
                                                     float4* __restrict__ xt, float4* __restrict__ box) {
   __shared__ double sh[5 * 8];
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(128) k_ff_tblocks(const double4* __restrict__ 
   const int64_t i = b * kTargetBlock + t;
   float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
   if (tslot[i] >= 0) {
-    const double4 p = tgt[tslot[i]];
+    const double4_16a p = tgt[tslot[i]];
     x = make_float4(float(p.x), float(p.y), float(p.z), 1.f);
   }
   xt[i] = x;
@@ -355,10 +355,10 @@ __global__ void __launch_bounds__(128) k_ff_eval(
       __syncthreads();
       const u64 X2 = pk2(x.x, x.x), Y2 = pk2(x.y, x.y), Z2 = pk2(x.z, x.z), C02 = pk2(c0, c0);
       u64 W0 = 0ull, W1 = 0ull, W2 = 0ull;
-      const ulonglong4* pr = reinterpret_cast<const ulonglong4*>(buf);
+      const ulonglong4_16a* pr = reinterpret_cast<const ulonglong4_16a*>(buf);
 #pragma unroll 4
       for (int i = 0; i < (o + 1) >> 1; ++i) {
-        const ulonglong4 s = pr[i];  // (x0 x1) (y0 y1) (z0 z1) (g0 g1)
+        const ulonglong4_16a s = pr[i];  // (x0 x1) (y0 y1) (z0 z1) (g0 g1)
         const u64 dx = sub2(X2, s.x), dy = sub2(Y2, s.y), dz = sub2(Z2, s.z);
         const u64 q = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, C02)));
         float qa, qb;
@@ -440,10 +440,10 @@ void ff_cells(lpm_context& ctx, const float4* ys, const int4* cells, int ncells,
 void ff_launch_tree(lpm_context& ctx, FFDevice& d, const void* tgt, const void* src, double* wout,
                     int64_t wstride, double c0, double theta, double rho_min, bool learn) {
   cudaStream_t st = ctx.stream;
-  k_ff_sort_src<<<unsigned((d.nsrc + 255) / 256), 256, 0, st>>>(static_cast<const double4*>(src),
+  k_ff_sort_src<<<unsigned((d.nsrc + 255) / 256), 256, 0, st>>>(static_cast<const double4_16a*>(src),
                                                                  d.perm, d.nsrc, d.ys);
   k_ff_cells<<<d.ncells, 128, 0, st>>>(d.ys, d.cells, d.ncells, float(theta), d.rmax, d.cd);
-  k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4*>(tgt), d.tslot,
+  k_ff_tblocks<<<unsigned(d.nblocks), 128, 0, st>>>(static_cast<const double4_16a*>(tgt), d.tslot,
                                                     d.xt, d.box);
   k_ff_lists<<<unsigned((d.nblocks + 63) / 64), 64, 0, st>>>(d.cd, d.cells, d.box, d.nblocks,
                                                             float(theta), float(rho_min), learn,

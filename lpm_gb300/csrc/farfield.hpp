@@ -89,7 +89,7 @@ struct lpm_farfield {
   bool built() const;
   // w[c * wstride + t] = sum over sources of g (x_t - y) / (|x_t - y|^2 + c0)
   // up to terms parallel to x_t (the chord-form sum whose cross product with
-  // x_t gives the velocity), for packed double4 targets (x, y, z, _) and
+  // x_t gives the velocity), for packed double4_16a targets (x, y, z, _) and
   // sources (x, y, z, g) in the order given to build().
   void evaluate(const void* tgt, const void* src, double* wout, int64_t wstride, double c0,
                 double eps);

@@ -19,17 +19,17 @@ using lpm::fail;
 
 __global__ void k_ff_pack_src(lpm::View fx, const double* __restrict__ zeta,
                               const double* __restrict__ area, const int* __restrict__ src2slot,
-                              int64_t ns, double4* __restrict__ src) {
+                              int64_t ns, double4_16a* __restrict__ src) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (k >= ns) return;
   const int64_t s = src2slot[k];
-  src[k] = make_double4(fx(s, 0), fx(s, 1), fx(s, 2), zeta[s] * area[s]);
+  src[k] = make_double4_16a(fx(s, 0), fx(s, 1), fx(s, 2), zeta[s] * area[s]);
 }
 
-__global__ void k_ff_pack_tgt(lpm::View x, int64_t n, double4* __restrict__ tgt) {
+__global__ void k_ff_pack_tgt(lpm::View x, int64_t n, double4_16a* __restrict__ tgt) {
   const int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
-  tgt[i] = make_double4(x(i, 0), x(i, 1), x(i, 2), 0.0);
+  tgt[i] = make_double4_16a(x(i, 0), x(i, 1), x(i, 2), 0.0);
 }
 
 // u = -(1/2pi) w cross x
@@ -170,7 +170,7 @@ int lpm_farfield_velocity(lpm_farfield* ff, lpm_view u, lpm_view x, int64_t nx, 
     cudaSetDevice(c.device);
     c.arena.reset();
     c.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
-                    sizeof(double4) * size_t(nf + nx) + sizeof(double) * 3 * size_t(nx) + 8192);
+                    sizeof(double4_16a) * size_t(nf + nx) + sizeof(double) * 3 * size_t(nx) + 8192);
     int* slot2src = static_cast<int*>(c.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
     int* src2slot = static_cast<int*>(c.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
     const int64_t ns = lpm::compact_sources(c, mask, nf, slot2src, src2slot);
@@ -180,16 +180,16 @@ int lpm_farfield_velocity(lpm_farfield* ff, lpm_view u, lpm_view x, int64_t nx, 
       LPM_CUDA(cudaGetLastError());
       return LPM_OK;
     }
-    double4* src = static_cast<double4*>(c.arena.take(sizeof(double4) * ns));
-    double4* tgt = static_cast<double4*>(c.arena.take(sizeof(double4) * nx));
+    double4_16a* src = static_cast<double4_16a*>(c.arena.take(sizeof(double4_16a) * ns));
+    double4_16a* tgt = static_cast<double4_16a*>(c.arena.take(sizeof(double4_16a) * nx));
     double* w = static_cast<double*>(c.arena.take(sizeof(double) * 3 * nx));
     k_ff_pack_src<<<unsigned((ns + 255) / 256), 256, 0, c.stream>>>(lpm::to_view(fx), zeta, area,
                                                                      src2slot, ns, src);
     k_ff_pack_tgt<<<unsigned((nx + 255) / 256), 256, 0, c.stream>>>(lpm::to_view(x), nx, tgt);
     c.launches += 2;
-    std::vector<double4> hs(ns), ht(nx);
-    LPM_CUDA(cudaMemcpyAsync(hs.data(), src, sizeof(double4) * ns, cudaMemcpyDeviceToHost, c.stream));
-    LPM_CUDA(cudaMemcpyAsync(ht.data(), tgt, sizeof(double4) * nx, cudaMemcpyDeviceToHost, c.stream));
+    std::vector<double4_16a> hs(ns), ht(nx);
+    LPM_CUDA(cudaMemcpyAsync(hs.data(), src, sizeof(double4_16a) * ns, cudaMemcpyDeviceToHost, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(ht.data(), tgt, sizeof(double4_16a) * nx, cudaMemcpyDeviceToHost, c.stream));
     LPM_CUDA(cudaStreamSynchronize(c.stream));
     std::vector<double> sx(3 * ns), tx(3 * nx);
     for (int64_t i = 0; i < ns; ++i) sx[3 * i] = hs[i].x, sx[3 * i + 1] = hs[i].y, sx[3 * i + 2] = hs[i].z;

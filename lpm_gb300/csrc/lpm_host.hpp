@@ -165,8 +165,8 @@ struct NbodyPlan {
 };
 NbodyPlan plan_nbody(lpm_context& ctx, int precision, int ndim, int form,
                      bool wu, bool wp, int64_t ntgt, int64_t nsrc);
-// tgt: float4[ntgt_pad] (FP32) or double4[ntgt_pad] (FP64, with tself);
-// src: float4/double4[nsrc_pad].  eps: kernel smoothing.
+// tgt: float4[ntgt_pad] (FP32) or double4_16a[ntgt_pad] (FP64, with tself);
+// src: float4/double4_16a[nsrc_pad].  eps: kernel smoothing.
 void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
                   const int* tself, const void* src, double* part,
                   double eps);

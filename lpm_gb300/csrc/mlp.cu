@@ -451,13 +451,13 @@ __device__ __forceinline__ double unif(uint64_t h) { return double(h >> 11) * (1
 // residual velocity, stored in the target's canonical frame and normalised.
 __global__ void __launch_bounds__(128) k_ff_samples(const float* __restrict__ cd,
                                                     const int4* __restrict__ cells,
-                                                    const double4* __restrict__ ysd,
+                                                    const double4_16a* __restrict__ ysd,
                                                     const int* __restrict__ jobs, int njobs,
                                                     uint64_t seed, float theta, float rho_min,
                                                     float eps, double c0, float* __restrict__ X,
                                                     float* __restrict__ Y, int64_t row0,
                                                     int64_t nrows) {
-  __shared__ double4 buf[256];
+  __shared__ double4_16a buf[256];
   const int job = blockIdx.x;
   const int t = threadIdx.x;
   const int c = jobs[job];
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(128) k_ff_samples(const float* __restrict__ cd
     for (int i = t; i < m; i += 128) buf[i] = ysd[ci.x + j0 + i];
     __syncthreads();
     for (int i = 0; i < m; ++i) {
-      const double4 s = buf[i];
+      const double4_16a s = buf[i];
       const double d0 = x[0] - s.x, d1 = x[1] - s.y, d2 = x[2] - s.z;
       const double r = s.w / (d0 * d0 + d1 * d1 + d2 * d2 + c0);
       we[0] += r * d0;
@@ -1028,11 +1028,11 @@ std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
     const int64_t ns = int64_t(sg.size());
     TreeTopo tp = build_tree(sx.data(), ns, nullptr, 0, leaf_max);
     const int nc = int(tp.start.size());
-    std::vector<double4> sd(ns);
+    std::vector<double4_16a> sd(ns);
     std::vector<float4> sf(ns);
     for (int64_t k = 0; k < ns; ++k) {
       const int j = tp.perm[k];
-      sd[k] = make_double4(sx[3 * j], sx[3 * j + 1], sx[3 * j + 2], sg[j]);
+      sd[k] = make_double4_16a(sx[3 * j], sx[3 * j + 1], sx[3 * j + 2], sg[j]);
       sf[k] = make_float4(float(sd[k].x), float(sd[k].y), float(sd[k].z), float(sd[k].w));
     }
     std::vector<int4> ci(nc);
@@ -1051,12 +1051,12 @@ std::vector<float> lpm_farfield::train(const lpm::TrainCfg& cfg) {
     const int64_t cap = std::max<int64_t>(1, std::min<int64_t>((n - rows + 127) / 128, (n / 4 + 127) / 128));
     if (int64_t(jobs.size()) > cap) jobs.resize(size_t(cap));
     TrainBufs fb;
-    double4* dsd = static_cast<double4*>(fb.alloc(sizeof(double4) * ns));
+    double4_16a* dsd = static_cast<double4_16a*>(fb.alloc(sizeof(double4_16a) * ns));
     float4* dsf = static_cast<float4*>(fb.alloc(sizeof(float4) * ns));
     int4* dci = static_cast<int4*>(fb.alloc(sizeof(int4) * nc));
     float* dcd = static_cast<float*>(fb.alloc(sizeof(float) * kCellF * size_t(nc)));
     int* djobs = static_cast<int*>(fb.alloc(sizeof(int) * jobs.size()));
-    LPM_CUDA(cudaMemcpyAsync(dsd, sd.data(), sizeof(double4) * ns, cudaMemcpyHostToDevice, st));
+    LPM_CUDA(cudaMemcpyAsync(dsd, sd.data(), sizeof(double4_16a) * ns, cudaMemcpyHostToDevice, st));
     LPM_CUDA(cudaMemcpyAsync(dsf, sf.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, st));
     LPM_CUDA(cudaMemcpyAsync(dci, ci.data(), sizeof(int4) * nc, cudaMemcpyHostToDevice, st));
     LPM_CUDA(cudaMemcpyAsync(djobs, jobs.data(), sizeof(int) * jobs.size(), cudaMemcpyHostToDevice, st));

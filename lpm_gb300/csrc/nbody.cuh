@@ -189,7 +189,7 @@ struct TilePipe {
 // ---------------------------------------------------------------------------
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
-template <> struct Vec4<double> { using type = double4; };
+template <> struct Vec4<double> { using type = double4_16a; };
 
 // FP32 source record with every value duplicated, (x, x, y, y) (z, z, g, g),
 // so that the packed f32x2 instructions apply one source to two targets
@@ -202,7 +202,7 @@ __host__ __device__ inline SrcF32 make_src_f32(float x, float y, float z, float 
 }
 template <typename T> struct SrcRec;
 template <> struct SrcRec<float> { using type = SrcF32; };
-template <> struct SrcRec<double> { using type = double4; };
+template <> struct SrcRec<double> { using type = double4_16a; };
 
 __device__ __forceinline__ float chord_rcp(float q) { return rcp_approx(q); }
 __device__ __forceinline__ double chord_rcp(double q) { return 1.0 / q; }
@@ -412,9 +412,9 @@ __global__ void __launch_bounds__(NT, MINB)
 
 // ---------------------------------------------------------------------------
 // FP64 parity kernel.
-//   tgt:  double4 (x, y, z, unused) per target
+//   tgt:  double4_16a (x, y, z, unused) per target
 //   tself: per-target source index to skip (-1 = none)
-//   src:  double4 (x, y, z, g): g = (-zeta)*area for FORM_BVE (the reference's
+//   src:  double4_16a (x, y, z, g): g = (-zeta)*area for FORM_BVE (the reference's
 //         circ), zeta*area otherwise
 //   part: [chunk][comp][ntgt_pad]; comps = (WU ? NDIM : 0) + (WP ? 1 : 0)
 // ---------------------------------------------------------------------------
@@ -433,13 +433,13 @@ __device__ __forceinline__ double ddiv(double a, double b) {
 
 template <int FORM, bool WU, bool WP, int R, int NT, int TILE>
 __global__ void __launch_bounds__(NT)
-    nbody_f64(const double4* __restrict__ tgt, const int* __restrict__ tself,
-              const double4* __restrict__ src, int64_t ntgt_pad,
+    nbody_f64(const double4_16a* __restrict__ tgt, const int* __restrict__ tself,
+              const double4_16a* __restrict__ src, int64_t ntgt_pad,
               int64_t nsrc_pad, int chunk_len, double eps2,
               double* __restrict__ part, int* err) {
   constexpr int ND = (FORM == 2) ? 2 : 3;
   constexpr int NC = (WU ? ND : 0) + (WP ? 1 : 0);
-  __shared__ __align__(128) double4 sbuf[2 * TILE];
+  __shared__ __align__(128) double4_16a sbuf[2 * TILE];
   __shared__ __align__(8) uint64_t sbar[2];
 
   const int tid = threadIdx.x;
@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int64_t ti = tbase + r * NT + tid;
-    const double4 t = tgt[ti];
+    const double4_16a t = tgt[ti];
     x0[r] = t.x;
     x1[r] = t.y;
     x2[r] = t.z;
@@ -463,18 +463,18 @@ __global__ void __launch_bounds__(NT)
     for (int k = 0; k < NC; ++k) A[k][r] = 0.0;
   }
 
-  TilePipe<double4, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  TilePipe<double4_16a, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
   pipe.start();
   for (int t = 0; t < pipe.ntiles; ++t) {
     if (!pipe.acquire(t)) {
       pipe.drain(t, err);
       return;
     }
-    const double4* sm = pipe.tile(t);
+    const double4_16a* sm = pipe.tile(t);
     const int jbase = int(s0 + (int64_t)t * TILE);
 #pragma unroll 1
     for (int j = 0; j < TILE; ++j) {
-      const double4 s = sm[j];
+      const double4_16a s = sm[j];
       const int jg = jbase + j;
 #pragma unroll
       for (int r = 0; r < R; ++r) {

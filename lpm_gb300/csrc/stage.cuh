@@ -148,14 +148,14 @@ __device__ void pack(const TG& g, const PK& k, int64_t t, const double* p,
     if (src >= 0) static_cast<SrcF32*>(k.src)[src] = make_src_f32(r.x, r.y, r.z, gw);
   } else if (k.mode == M_C64) {
     const double gw = src >= 0 ? dm(z, area) : 0.0;
-    static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, self ? gw : 0.0);
-    if (src >= 0) static_cast<double4*>(k.src)[src] = make_double4(p[0], p[1], p2, gw);
+    static_cast<double4_16a*>(k.tgt)[t] = make_double4_16a(p[0], p[1], p2, self ? gw : 0.0);
+    if (src >= 0) static_cast<double4_16a*>(k.src)[src] = make_double4_16a(p[0], p[1], p2, gw);
   } else {
-    static_cast<double4*>(k.tgt)[t] = make_double4(p[0], p[1], p2, 0.0);
+    static_cast<double4_16a*>(k.tgt)[t] = make_double4_16a(p[0], p[1], p2, 0.0);
     k.tself[t] = self ? src : -1;
     if (src >= 0) {
       const double gg = (k.form == FORM_BVE) ? dm(-z, area) : dm(z, area);
-      static_cast<double4*>(k.src)[src] = make_double4(p[0], p[1], p2, gg);
+      static_cast<double4_16a*>(k.src)[src] = make_double4_16a(p[0], p[1], p2, gg);
     }
   }
 }
@@ -186,7 +186,7 @@ __device__ void combine_t(const PK& k, int64_t t, const double* p, double c0,
     const double gs = (double)static_cast<const float4*>(k.tgt)[t].w;
     chord_epilogue<M_C32, NDIM, true, WP>(a, p, gs, sg, c0, u, psi);
   } else {
-    const double gs = static_cast<const double4*>(k.tgt)[t].w;
+    const double gs = static_cast<const double4_16a*>(k.tgt)[t].w;
     chord_epilogue<M_C64, NDIM, true, WP>(a, p, gs, sg, c0, u, psi);
   }
 }

@@ -97,9 +97,9 @@ struct lpm_stepper_base {
     }
     plan = lpm::plan_nbody(c, precision, ndim, form, true, want_psi, T, nsrc);
     plan.skipc = skip_self;
-    const size_t rec = precision == LPM_FP32C ? 16 : 32;  // float4 / double4
+    const size_t rec = precision == LPM_FP32C ? 16 : 32;  // float4 / double4_16a
     tgt = dalloc(rec * plan.ntgt_pad);
-    src = dalloc(32 * plan.nsrc_pad);  // SrcF32 / double4
+    src = dalloc(32 * plan.nsrc_pad);  // SrcF32 / double4_16a
     tself = static_cast<int*>(dalloc(sizeof(int) * plan.ntgt_pad));
     part = static_cast<double*>(dalloc(plan.part_bytes()));
     sgbuf = static_cast<double*>(dalloc(sizeof(double) * (8 + 256)));
