@@ -66,8 +66,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if force or _stale(o, [s] + headers):
             # no contraction: the same FP64 results on x86-64 and aarch64 hosts,
             # and the on-device mesh generator reproduces the host mesh bitwise
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", *inc, "-c",
-                         str(s), "-o", str(o)])
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+                         *inc, "-c", str(s), "-o", str(o)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for cmd in jobs:
@@ -75,7 +75,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                     print(" ".join(cmd), flush=True)
             list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
-        cmd = [nv, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        cmd = [nv, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         _run(cmd)

@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <numeric>
 #include <stdexcept>
+#include <thread>
 #include <vector>
 
 #include "farfield.hpp"
@@ -70,10 +71,39 @@ uint64_t key_of(const Box& bx, const double* p) {
   return k;
 }
 
+// Sorts (key, index) pairs on up to 16 host threads: equal chunks sorted
+// concurrently, then merged pairwise.  The pairs are totally ordered (ties
+// in key broken by index), so the result is the single-threaded one.
+void parallel_sort(std::vector<std::pair<uint64_t, int>>& v) {
+  const int64_t n = int64_t(v.size());
+  const int hw = int(std::min(16u, std::max(1u, std::thread::hardware_concurrency())));
+  if (n < (int64_t(1) << 16) || hw == 1) {
+    std::sort(v.begin(), v.end());
+    return;
+  }
+  int p = 1;
+  while (p * 2 <= hw) p *= 2;
+  std::vector<int64_t> cut(p + 1);
+  for (int i = 0; i <= p; ++i) cut[i] = n * i / p;
+  std::vector<std::thread> th;
+  for (int i = 0; i < p; ++i)
+    th.emplace_back([&v, &cut, i] { std::sort(v.begin() + cut[i], v.begin() + cut[i + 1]); });
+  for (auto& t : th) t.join();
+  for (int w = 1; w < p; w *= 2) {
+    th.clear();
+    for (int i = 0; i + w < p; i += 2 * w)
+      th.emplace_back([&v, &cut, i, w, p] {
+        std::inplace_merge(v.begin() + cut[i], v.begin() + cut[i + w],
+                           v.begin() + cut[std::min(i + 2 * w, p)]);
+      });
+    for (auto& t : th) t.join();
+  }
+}
+
 std::vector<int> sorted_order(const Box& bx, const double* p, int64_t n, std::vector<uint64_t>& keys) {
   std::vector<std::pair<uint64_t, int>> kv(n);
   for (int64_t i = 0; i < n; ++i) kv[i] = {key_of(bx, p + 3 * i), int(i)};
-  std::sort(kv.begin(), kv.end());
+  parallel_sort(kv);
   std::vector<int> perm(n);
   keys.resize(n);
   for (int64_t i = 0; i < n; ++i) {
