@@ -264,6 +264,10 @@ int lpm_plane_direct_sum(lpm_crd3 tgt, lpm_crd3 src, const double* zeta,
                          int precision, double* u_out, long long u_stride_i,
                          long long u_stride_c, double* psi_out,
                          void* cuda_stream);
+/* Frees the calling thread's cached contexts (all devices) after
+ * synchronising their streams; the next one-call form creates a new one.
+ * Call it before a host thread that used the one-call forms exits. */
+int lpm_one_call_release(void);
 /* One step of a stepper (the advance_timestep calls above under the step
  * names), and nsteps RK4 steps of every problem of an ensemble. */
 int lpm_bve_rk4_step(lpm_bve_rk4* st, lpm_view vx, double* vzeta,

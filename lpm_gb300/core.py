@@ -66,6 +66,7 @@ EXPORTS = [
     "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
+    "lpm_one_call_release",
 ]
 
 
@@ -177,6 +178,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_bve_rk4_step": [vp, V, vp, V, V, vp, V, vp, vp],
         "lpm_ic2d_rk2_step": [vp, V, vp, V, vp, V, vp, V, vp, vp, vp],
         "lpm_ensemble_run": [vp, i32, V, vp, V, V, vp, V, vp],
+        "lpm_one_call_release": [],
         "lpm_vtk_write_polymesh": [C.c_char_p, i32, i64, vp, vp, i64, i32, vp, vp, vp, i32, vp],
     }
     for name, args in sig.items():

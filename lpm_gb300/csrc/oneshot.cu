@@ -2,11 +2,12 @@
 // lpm_context: a direct sum given coordinate views, a precision and a CUDA
 // stream, and step/run forms of the steppers and the ensemble.
 //
-// The direct-sum calls use a context cached per host thread and device
-// (created on first use, never destroyed: it lives as long as the thread).
-// Calls are stream-ordered on the stream they are given; when a thread
-// switches streams, the previous stream is synchronised first, because the
-// context's scratch memory is reused by the next call.
+// The direct-sum calls use a context cached per host thread and device,
+// created on first use and freed by lpm_one_call_release (its scratch memory
+// can be large: the FP64 chunk partials of the last call).  Calls are
+// stream-ordered on the stream they are given; when a thread switches
+// streams, the previous stream is synchronised first, because the context's
+// scratch memory is reused by the next call.
 #include <cmath>
 
 #include <cuda_runtime.h>
@@ -104,6 +105,16 @@ int lpm_plane_direct_sum(lpm_crd3 tgt, lpm_crd3 src, const double* zeta, const d
   } catch (...) {
     return lpm::handle_exception();
   }
+}
+
+int lpm_one_call_release(void) {
+  int status = LPM_OK;
+  for (int d = 0; d < kMaxDevices; ++d) {
+    if (!t_ctx[d]) continue;
+    if (int r = lpm_context_destroy(t_ctx[d])) status = r;
+    t_ctx[d] = nullptr;
+  }
+  return status;
 }
 
 int lpm_bve_rk4_step(lpm_bve_rk4* st, lpm_view vx, double* vzeta, lpm_view vvel, lpm_view fx,

@@ -304,3 +304,13 @@ def test_one_call_direct_sums(gpu_ctx, precision):
                     fa_, fb_ = torch.isfinite(a), torch.isfinite(b)
                     assert torch.equal(fa_, fb_), (kind, eps, coll)
                     assert torch.equal(a[fa_], b[fb_]), (kind, eps, coll)
+    # releasing the thread's cached context frees it; the next call makes a new one
+    check(lib().lpm_one_call_release())
+    u3 = torch.zeros_like(u1)
+    p3 = torch.zeros_like(p1)
+    with torch.cuda.stream(stream):
+        check(fn(crd3(tgt), crd3(T["fx"]), ptr(T["z"]), ptr(T["fa"]), ptr(T["fm"]), fx.shape[0],
+                 coll, eps, 3, prec, ptr(u3), ndim, 1, ptr(p3), C.c_void_p(stream.cuda_stream)))
+    stream.synchronize()
+    assert torch.equal(u3, u1) and torch.equal(p3, p1)
+    check(lib().lpm_one_call_release())

@@ -52,6 +52,7 @@ def test_one_call_argument_checks():
         d = core.Crd3(None, 5, 3, 1)
         assert fn(d, c, None, None, None, 0, 1, 0.0, 1, core.FP64, None, 3, 1, None, None) \
             == core.LPM_ERR_ARG  # collocated with a different target view
+    assert L.lpm_one_call_release() == core.LPM_OK  # nothing cached: a no-op
     v = core.View(None, 0, 0)
     assert L.lpm_ensemble_run(None, -1, v, None, v, v, None, v, None) == core.LPM_ERR_ARG
     assert L.lpm_ensemble_run(None, 0, v, None, v, v, None, v, None) == core.LPM_OK
