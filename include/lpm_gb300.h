@@ -46,10 +46,17 @@ extern "C" {
 #define LPM_ERR_STATE (-5)   /* object used in the wrong state */
 
 /* ---- arithmetic of the pairwise sum ------------------------------------ */
-/* LPM_FP64: every pair term in FP64 in the reference's evaluation order.
+/* LPM_FP64: the reference's pair kernels in FP64 (1 - x.y [+ eps^2] on the
+ *            sphere, |x-y|^2 + eps^2 on the plane) with the cross product
+ *            taken out of the sum (u = x cross sum_j (g_j / arg_j) y_j) and one
+ *            Newton-Raphson quotient per pair; within 1e-12 of the reference.
+ * LPM_FP64_EXACT: every pair term in FP64 in the reference's evaluation
+ *            order (correctly rounded divisions), each term equal to the
+ *            reference's bit for bit; about 3x slower than LPM_FP64.
  * LPM_FP32C: FP32 pair kernel (denominator rebuilt as |x-y|^2/2 + eps^2),
  *            per-tile Kahan/TwoSum-compensated sums, FP64 epilogue. */
 #define LPM_FP64 64
+#define LPM_FP64_EXACT 66
 #define LPM_FP32C 32
 /* LPM_FP64_CHORD: the LPM_FP32C algorithm (chord denominator, cross product
  * hoisted out of the sum) in FP64.  On unit vectors it equals LPM_FP64 to
@@ -77,7 +84,8 @@ int lpm_context_create(lpm_context** ctx, int device);
 int lpm_context_destroy(lpm_context* ctx);
 /* cudaStream_t passed as void*; 0 = the legacy default stream. */
 int lpm_context_set_stream(lpm_context* ctx, void* cuda_stream);
-/* LPM_FP64 (default) or LPM_FP32C for the functor entry points below. */
+/* LPM_FP64 (default), LPM_FP64_EXACT, LPM_FP64_CHORD or LPM_FP32C for the
+ * functor entry points below. */
 int lpm_context_set_precision(lpm_context* ctx, int precision);
 /* Waits for the context's stream, then reports LPM_ERR_TIMEOUT if a bounded
  * device-side wait gave up since the last check (and clears the flag). */
@@ -285,7 +293,8 @@ int lpm_ic2d_rk2_step(lpm_ic2d_rk2* st, lpm_view vx, double* vzeta,
  * face slots (fixed).  precision: LPM_FP32C or LPM_FP64_CHORD (chord form,
  * velocity only).  Each evaluation is one persistent launch over (problem,
  * target block, source chunk) work items; a step is replayed from a CUDA
- * graph; the chunk length is autotuned on the first call. */
+ * graph; the chunk length and the FP32 kernel shape (threads x targets per
+ * thread) are autotuned on the first call. */
 typedef struct lpm_ensemble lpm_ensemble;
 int lpm_ensemble_create(lpm_context* ctx, lpm_ensemble** out, int nproblems,
                         const int64_t* nverts, const int64_t* nfaces,
@@ -305,6 +314,8 @@ int lpm_ensemble_advance_timestep(lpm_ensemble* e, lpm_view vx, double* vzeta,
 int lpm_ensemble_info(lpm_ensemble* e, int64_t* chunk_len, int64_t* items,
                       int64_t* targets);
 int lpm_ensemble_nbody_time(lpm_ensemble* e, double* ms, int64_t* launches);
+/* Kernel shape in use: threads per CTA and targets per thread. */
+int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread);
 /* Fixes the chunk length (sources; rounded up to whole tiles) instead of
  * autotuning it, e.g. for bitwise-reproducible runs across ensembles.  Call
  * before the first velocity/step call. */
@@ -349,6 +360,15 @@ int lpm_ic_eval(int kind, const double* params, int nparams, int ndim,
                 int64_t n, const double* x, double* zeta);
 
 /* ---- instrumentation ----------------------------------------------------- */
+/* Test of the failure path, no counterpart in the reference (whose device
+ * checks abort, src/lpm_assert.hpp:32-46).  Launches one CTA on the context's
+ * stream whose tile wait cannot complete (its mbarrier expects a copy that is
+ * never issued); after spin_limit polls (1 to 2^20) it sets the context's
+ * timeout flag and returns without touching global memory, exactly as an
+ * N-body kernel does when a tile copy never lands.  The next
+ * lpm_context_synchronize reports LPM_ERR_TIMEOUT and clears the flag; the
+ * context stays usable. */
+int lpm_wait_selftest(lpm_context* ctx, int spin_limit);
 /* Measured FP32 / FP64 FMA peak of this GPU (TFLOP/s) from a short
  * register-only microbenchmark; synchronous. */
 int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops);

@@ -15,10 +15,10 @@ ABI in ``include/lpm_gb300.h``; this package is its Python host layer:
 - ``partition`` target and problem sharding across ranks
 - ``build``     nvcc build of the library
 """
-from .core import (FP32C, FP64, FP64_CHORD, PLANE, SPHERE, Context, LpmError, build_mesh,
+from .core import (FP32C, FP64, FP64_CHORD, FP64_EXACT, PLANE, SPHERE, Context, LpmError, build_mesh,
                    build_mesh_device, default_context, eval_ic, lib, mesh_face_vertices,
                    mesh_sizes)
 
-__all__ = ["FP32C", "FP64", "FP64_CHORD", "PLANE", "SPHERE", "Context", "LpmError",
+__all__ = ["FP32C", "FP64", "FP64_CHORD", "FP64_EXACT", "PLANE", "SPHERE", "Context", "LpmError",
            "build_mesh", "build_mesh_device", "default_context", "eval_ic", "lib",
            "mesh_face_vertices", "mesh_sizes"]

@@ -23,6 +23,7 @@ LPM_ERR_STATE = -5
 FP64 = 64
 FP32C = 32
 FP64_CHORD = 65
+FP64_EXACT = 66
 PLANE = 2
 SPHERE = 3
 
@@ -66,7 +67,7 @@ EXPORTS = [
     "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
-    "lpm_one_call_release",
+    "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape",
 ]
 
 
@@ -113,6 +114,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_context_set_stream": [vp, vp],
         "lpm_context_set_precision": [vp, i32],
         "lpm_context_synchronize": [vp],
+        "lpm_wait_selftest": [vp, i32],
         "lpm_context_kernel_launches": [vp],
         "lpm_last_error": [],
         "lpm_device_count": [],
@@ -147,6 +149,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ensemble_velocity": [vp, V, V, V, vp, V, vp],
         "lpm_ensemble_advance_timestep": [vp, V, vp, V, V, vp, V, vp],
         "lpm_ensemble_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)],
+        "lpm_ensemble_shape": [vp, C.POINTER(i32), C.POINTER(i32)],
         "lpm_ensemble_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ensemble_set_chunk_len": [vp, i64],
         "lpm_sphere_tangency": [vp, vp, V, V, i64],

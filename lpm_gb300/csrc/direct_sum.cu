@@ -189,7 +189,7 @@ template <int MODE, int NDIM, bool WU, bool WP>
 __global__ void k_combine(const double* __restrict__ part, int nchunks,
                           int64_t ntgt_pad, int64_t off, int64_t n, View x,
                           View u, double* psi, const void* tgt,
-                          const double* sg, double c0) {
+                          const double* sg, double c0, int form, bool exact) {
   constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -202,14 +202,21 @@ __global__ void k_combine(const double* __restrict__ part, int nchunks,
 #pragma unroll
     for (int k = 0; k < NC; ++k) a[k] += p[k * ntgt_pad];
   }
+  double pos[3] = {x(i, 0), x(i, 1), NDIM == 3 ? x(i, 2) : 0.0};
   if (MODE == M_REF64) {
+    double uu[3], ps = 0;
+    if (exact) {
+      for (int k = 0; k < NDIM; ++k) uu[k] = a[k];
+      ps = a[NC - 1];
+    } else {
+      ref64_epilogue<NDIM, WU, WP>(a, pos, form, uu, &ps);
+    }
     if (WU)
 #pragma unroll
-      for (int k = 0; k < NDIM; ++k) u(i, k) = a[k];
-    if (WP) psi[i] = a[NC - 1];
+      for (int k = 0; k < NDIM; ++k) u(i, k) = uu[k];
+    if (WP) psi[i] = ps;
     return;
   }
-  double pos[3] = {x(i, 0), x(i, 1), NDIM == 3 ? x(i, 2) : 0.0};
   double uu[3], ps = 0;
   const double gs = MODE == M_C32 ? (double)static_cast<const float4*>(tgt)[t].w
                                   : static_cast<const double4_16a*>(tgt)[t].w;
@@ -227,7 +234,8 @@ void launch_combine(lpm_context& ctx, const NbodyPlan& p, const double* part,
   const int th = 256;
   const int64_t nb = (seg.n + th - 1) / th;
   k_combine<MODE, NDIM, WU, WP><<<nb, th, 0, ctx.stream>>>(
-      part, p.nchunks, p.ntgt_pad, off, seg.n, seg.x, seg.u, seg.psi, tgt, sg, c0);
+      part, p.nchunks, p.ntgt_pad, off, seg.n, seg.x, seg.u, seg.psi, tgt, sg, c0, p.form,
+      ref64_exact(p.precision));
   ctx.launches++;
 }
 
@@ -296,9 +304,14 @@ template <int FORM, bool WU, bool WP>
 void launch_f64(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
                 const int* tself, const void* src, double* part, double eps2) {
   dim3 grid(unsigned(p.ntgt_pad / (F64_NT * F64_R)), unsigned(p.nchunks));
-  nbody_f64<FORM, WU, WP, F64_R, F64_NT, F64_TILE><<<grid, F64_NT, 0, ctx.stream>>>(
-      static_cast<const double4_16a*>(tgt), tself, static_cast<const double4_16a*>(src),
-      p.ntgt_pad, p.nsrc_pad, p.chunk_len, eps2, part, ctx.d_err);
+  if (ref64_exact(p.precision))
+    nbody_f64<FORM, WU, WP, F64_R, F64_NT, F64_TILE><<<grid, F64_NT, 0, ctx.stream>>>(
+        static_cast<const double4_16a*>(tgt), tself, static_cast<const double4_16a*>(src),
+        p.ntgt_pad, p.nsrc_pad, p.chunk_len, eps2, part, ctx.d_err);
+  else
+    nbody_f64h<FORM, WU, WP, F64_R, F64_NT, F64_TILE><<<grid, F64_NT, 0, ctx.stream>>>(
+        static_cast<const double4_16a*>(tgt), tself, static_cast<const double4_16a*>(src),
+        p.ntgt_pad, p.nsrc_pad, p.chunk_len, eps2, part, ctx.d_err);
   ctx.launches++;
 }
 
@@ -337,7 +350,7 @@ int occupancy(int precision) {
           &v, nbody_chord<double, 3, true, false, false, F64_R, F64_NT, F64_TILE, 4>, F64_NT, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &v, nbody_f64<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
+          &v, nbody_f64h<0, true, false, F64_R, F64_NT, F64_TILE>, F64_NT, 0);
     o = v > 0 ? v : 1;
   }
   return o;
@@ -769,6 +782,33 @@ void err_norms(lpm_context& ctx, int ndim, int64_t n, View appx, View exact,
   out[0] = r[0] * safe(r[1]);
   out[1] = std::sqrt(r[2] * safe(r[3]));
   out[2] = r[4] * safe(r[5]);
+}
+
+namespace {
+// The failure path of every N-body kernel (TilePipe::acquire giving up, then
+// TilePipe::drain): thread 0 announces a tile whose bytes never arrive, the
+// bounded wait runs out, the CTA flags the error and leaves.  No global
+// memory is read; the pipe's source pointer is never dereferenced.
+__global__ void k_wait_selftest(unsigned spin, int* err) {
+  constexpr int TILE = 16;
+  __shared__ __align__(128) double4_16a sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+  TilePipe<double4_16a, TILE> pipe{sbuf, sbar, nullptr, 1};
+  pipe.spin = spin;
+  pipe.init();
+  if (threadIdx.x == 0) mbar_expect_tx(&sbar[0], TILE * sizeof(double4_16a));
+  if (!pipe.acquire(0)) {
+    pipe.drain(0, err);
+    return;
+  }
+  pipe.release(0);
+}
+}  // namespace
+
+void wait_selftest(lpm_context& ctx, unsigned spin) {
+  k_wait_selftest<<<1, 32, 0, ctx.stream>>>(spin, ctx.d_err);
+  ctx.launches++;
+  LPM_CUDA(cudaGetLastError());
 }
 
 double fma_peak(lpm_context& ctx, int precision) {

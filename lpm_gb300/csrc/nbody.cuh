@@ -22,8 +22,15 @@
 // tile's plain FP32 partial is merged with an error-free TwoSum, so the
 // compensation costs O(1/TILE) per pair.
 //
-// FP64 path (parity form).  Every pair term is computed with the reference's
-// formula and operation order using non-contracting intrinsics
+// FP64 path (LPM_FP64, parity form within 1e-12).  The reference's kernels
+// (1 - x.y [+ eps^2] on the sphere, |x - y|^2 + eps^2 on the plane) with the
+// cross product hoisted out of the sum: per target B = sum_j (g_j / arg_j) y_j
+// and u = s (x cross B) in the epilogue; one quotient per pair by Newton's
+// method from the hardware's approximate reciprocal.  11 FP64 operations per
+// sphere pair (eps form), against ~32 with three correctly rounded divisions.
+//
+// FP64 exact path (LPM_FP64_EXACT).  Every pair term is computed with the
+// reference's formula and operation order using non-contracting intrinsics
 // (__dmul_rn/__dadd_rn/__ddiv_rn), so each term equals the reference's term
 // bit for bit; only the grouping of the sum differs.
 #pragma once
@@ -101,10 +108,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// Returns false if the phase did not complete within kSpinLimit tries.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar,
-                                                  unsigned parity) {
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
+// Returns false if the phase did not complete within `limit` tries.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity,
+                                                  unsigned limit = kSpinLimit) {
+  for (unsigned it = 0; it < limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
   }
   return false;
@@ -131,6 +138,7 @@ struct TilePipe {
   int ntiles;
   unsigned g0 = 0;  // tiles this CTA consumed before the chunk (a persistent
                     // CTA keeps the barriers' phases running across chunks)
+  unsigned spin = kSpinLimit;  // polls per wait before giving up
 
   __device__ void init() {
     if (threadIdx.x == 0) {
@@ -158,7 +166,7 @@ struct TilePipe {
   // Waits for tile t; returns false (CTA-uniform) if the wait gave up.
   __device__ bool acquire(int t) {
     const unsigned g = g0 + t;
-    const bool ok = mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1);
+    const bool ok = mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1, spin);
     return !__syncthreads_or(!ok);
   }
   // All threads are done with tile t: refill its buffer with tile t + 2.
@@ -172,7 +180,7 @@ struct TilePipe {
       atomicExch(err, 1);
       for (int k = t; k < t + 2 && k < ntiles; ++k) {
         const unsigned g = g0 + k;
-        (void)mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1);
+        (void)mbar_wait_bounded(&bar[g & 1], (g >> 1) & 1, spin);
       }
     }
   }
@@ -543,14 +551,162 @@ __global__ void __launch_bounds__(NT)
     for (int r = 0; r < R; ++r) out[k * ntgt_pad + tbase + r * NT + tid] = A[k][r];
 }
 
+// ---------------------------------------------------------------------------
+// FP64 kernel, cross product hoisted (LPM_FP64).
+//   tgt, tself, src: as nbody_f64.
+//   sphere forms (FORM 0 = BVE, g = (-zeta) A, eps = 0; FORM 1 = eps kernel,
+//   g = zeta A): arg_j = (1 - x.y_j) + eps^2,
+//     partials  B = sum_j (g_j / arg_j) y_j   [WU, 3 components]
+//               L = sum_j g_j log(arg_j)      [WP]
+//   and ref64_epilogue forms u = s (x cross B), psi = s L with s = 1/(4 pi)
+//   (BVE: biot_savart, greens_fn) or -1/(4 pi) (kernel_vals).
+//   plane (FORM 2): m = x - y_j, arg_j = (m.m) + eps^2,
+//     A = sum_j (g_j / arg_j) (-m_1, m_0),  L = sum_j g_j log(arg_j),
+//   u = A / (2 pi), psi = -L / (4 pi).
+// The skipped pair (i == j) is selected out, so a non-finite quotient of a
+// coincident pair never enters the sum.
+// ---------------------------------------------------------------------------
+
+// n / d from the PTX approximate FP64 reciprocal r (relative error e0 of
+// about 2^-20 or less): with e = 1 - d r (exact to rounding, one fused
+// multiply-add), n / d = n r / (1 - e) = n r (1 + e + e^2) + O(e0^3), so
+// q = q0 + q0 (e + e^2), q0 = n r -- the second-order Newton-Raphson
+// (Halley-type) correction of the quotient, four FP64 operations.  Within
+// about one ulp of n / d for the finite, normal d that occur here; d = 0
+// gives NaN.
+__device__ __forceinline__ double div_nr(double n, double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  const double q0 = n * r;
+  const double e = fma(-d, r, 1.0);
+  return fma(q0, fma(e, e, e), q0);
+}
+
+template <int FORM, bool WU, bool WP, int R, int NT, int TILE>
+__global__ void __launch_bounds__(NT)
+    nbody_f64h(const double4_16a* __restrict__ tgt, const int* __restrict__ tself,
+               const double4_16a* __restrict__ src, int64_t ntgt_pad,
+               int64_t nsrc_pad, int chunk_len, double eps2,
+               double* __restrict__ part, int* err) {
+  constexpr int ND = (FORM == 2) ? 2 : 3;
+  constexpr int NC = (WU ? ND : 0) + (WP ? 1 : 0);
+  __shared__ __align__(128) double4_16a sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+
+  const int tid = threadIdx.x;
+  const int64_t tbase = (int64_t)blockIdx.x * (NT * R);
+  const int64_t s0 = (int64_t)blockIdx.y * chunk_len;
+  int64_t slen = nsrc_pad - s0;
+  if (slen > chunk_len) slen = chunk_len;
+
+  double x0[R], x1[R], x2[R];
+  int self[R];
+  double A[NC][R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int64_t ti = tbase + r * NT + tid;
+    const double4_16a t = tgt[ti];
+    x0[r] = t.x;
+    x1[r] = t.y;
+    x2[r] = t.z;
+    self[r] = tself[ti];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) A[k][r] = 0.0;
+  }
+
+  TilePipe<double4_16a, TILE> pipe{sbuf, sbar, src + s0, int(slen / TILE)};
+  pipe.start();
+  for (int t = 0; t < pipe.ntiles; ++t) {
+    if (!pipe.acquire(t)) {
+      pipe.drain(t, err);
+      return;
+    }
+    const double4_16a* sm = pipe.tile(t);
+    const int jbase = int(s0 + (int64_t)t * TILE);
+#pragma unroll 2
+    for (int j = 0; j < TILE; ++j) {
+      const double4_16a s = sm[j];
+      const int jg = jbase + j;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const bool skip = (jg == self[r]);
+        double arg;
+        double m0 = 0.0, m1 = 0.0;
+        if (FORM == 2) {
+          m0 = x0[r] - s.x;
+          m1 = x1[r] - s.y;
+          arg = fma(m0, m0, fma(m1, m1, eps2));
+        } else {
+          // x.y - 1 accumulated from the -1 on, so 1 - x.y [+ eps^2] costs
+          // no separate subtraction
+          const double dm1 = fma(x2[r], s.z, fma(x1[r], s.y, fma(x0[r], s.x, -1.0)));
+          arg = (FORM == 1) ? eps2 - dm1 : -dm1;
+        }
+        if (WU) {
+          const double q = div_nr(s.w, arg);
+          const double g = skip ? 0.0 : q;
+          if (FORM == 2) {
+            A[0][r] = fma(-m1, g, A[0][r]);
+            A[1][r] = fma(m0, g, A[1][r]);
+          } else {
+            A[0][r] = fma(g, s.x, A[0][r]);
+            A[1][r] = fma(g, s.y, A[1][r]);
+            A[2][r] = fma(g, s.z, A[2][r]);
+          }
+        }
+        if (WP) {
+          const double l = fma(log(arg), s.w, A[NC - 1][r]);
+          A[NC - 1][r] = skip ? A[NC - 1][r] : l;
+        }
+      }
+    }
+    pipe.release(t);
+  }
+
+  double* out = part + (int64_t)blockIdx.y * NC * ntgt_pad;
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[k * ntgt_pad + tbase + r * NT + tid] = A[k][r];
+}
+
+// Epilogue of the hoisted FP64 kernel for one target: a = summed partials,
+// p = the FP64 position the target was evaluated at, form = FORM_*.
+template <int NDIM, bool WU, bool WP>
+__device__ __forceinline__ void ref64_epilogue(const double* a, const double* p, int form,
+                                               double* u, double* psi) {
+  constexpr int NC = (WU ? NDIM : 0) + (WP ? 1 : 0);
+  constexpr double INV4PI = 1.0 / (4.0 * kPI);
+  constexpr double INV2PI = 1.0 / (2.0 * kPI);
+  if (NDIM == 3) {
+    const double s = form == 0 ? INV4PI : -INV4PI;
+    if (WU) {
+      u[0] = s * (p[1] * a[2] - p[2] * a[1]);
+      u[1] = s * (p[2] * a[0] - p[0] * a[2]);
+      u[2] = s * (p[0] * a[1] - p[1] * a[0]);
+    }
+    if (WP) *psi = s * a[NC - 1];
+  } else {
+    if (WU) {
+      u[0] = INV2PI * a[0];
+      u[1] = INV2PI * a[1];
+    }
+    if (WP) *psi = -INV4PI * a[NC - 1];
+  }
+}
+
 // Arithmetic modes of the pair sum.
 enum Mode : int {
-  M_REF64 = 0,  // LPM_FP64: the reference's formulas, FP64
+  M_REF64 = 0,  // LPM_FP64 / LPM_FP64_EXACT: the reference's formulas, FP64
   M_C32 = 1,    // LPM_FP32C: chord form, FP32 pairs, compensated sums
   M_C64 = 2     // LPM_FP64_CHORD: chord form, FP64
 };
 __host__ __device__ inline int mode_of(int precision) {
   return precision == LPM_FP32C ? M_C32 : (precision == LPM_FP64_CHORD ? M_C64 : M_REF64);
+}
+// LPM_FP64 runs the hoisted kernel; LPM_FP64_EXACT the term-by-term kernel.
+__host__ __device__ inline bool ref64_exact(int precision) {
+  return precision == LPM_FP64_EXACT;
 }
 
 // Chord-form epilogue of one target: a = summed partials (w [, L]), p = the

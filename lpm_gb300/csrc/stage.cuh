@@ -76,6 +76,7 @@ struct EnsTg {
 // Packed tiles and partials of one problem's evaluations.
 struct Pk {
   int mode;  // M_REF64, M_C32 or M_C64
+  bool exact = false;  // M_REF64: term-by-term kernel (partials are u, psi)
   int form;
   bool skip_self;
   void* tgt;
@@ -96,6 +97,7 @@ struct Pk {
 // Packed tiles and partials of an ensemble: per-problem partial blocks.
 struct EnsPk {
   int mode;
+  bool exact = false;
   int form;
   bool skip_self;
   void* tgt;
@@ -178,8 +180,12 @@ __device__ void combine_t(const PK& k, int64_t t, const double* p, double c0,
     for (int m = 0; m < NC; ++m) a[m] += q[m * st];
   }
   if (k.mode == M_REF64) {
-    for (int m = 0; m < NDIM; ++m) u[m] = a[m];
-    if (WP) *psi = a[NDIM];
+    if (k.exact) {
+      for (int m = 0; m < NDIM; ++m) u[m] = a[m];
+      if (WP) *psi = a[NDIM];
+    } else {
+      ref64_epilogue<NDIM, true, WP>(a, p, k.form, u, psi);
+    }
     return;
   }
   if (k.mode == M_C32) {

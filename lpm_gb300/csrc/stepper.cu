@@ -144,6 +144,7 @@ struct lpm_stepper_base {
   lpm::Pk packs() const {
     lpm::Pk k;
     k.mode = lpm::mode_of(precision);
+    k.exact = lpm::ref64_exact(precision);
     k.form = form;
     k.skip_self = skip_self;
     k.tgt = tgt;
@@ -190,7 +191,7 @@ struct lpm_stepper_base {
       }
       return;
     }
-    if (precision != LPM_FP64 && want_psi && ndim == 3)
+    if (lpm::mode_of(precision) != lpm::M_REF64 && want_psi && ndim == 3)
       lpm::sum_strengths(*ctx, src, precision == LPM_FP32C, nsrc, sgbuf, sgbuf + 8);
     if (flags & LPM_STEP_TIME_NBODY) {
       cudaEvent_t e[2];
@@ -370,9 +371,11 @@ int lpm_bve_rk4_create(lpm_context* ctx, lpm_bve_rk4** out, int64_t nverts,
     if (!ctx || !out) return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: null argument");
     if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
       return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: sizes out of range");
-    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
+    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD &&
+        precision != LPM_FP64_EXACT)
       return lpm::fail(LPM_ERR_ARG,
-                       "lpm_bve_rk4_create: precision must be LPM_FP64, LPM_FP64_CHORD or LPM_FP32C");
+                       "lpm_bve_rk4_create: precision must be LPM_FP64, LPM_FP64_EXACT, "
+                       "LPM_FP64_CHORD or LPM_FP32C");
     if (!std::isfinite(dt) || !std::isfinite(Omega) || !std::isfinite(eps) || eps < 0)
       return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_create: non-finite dt/Omega or bad eps");
     auto* st = new lpm_bve_rk4();
@@ -397,6 +400,7 @@ int lpm_bve_rk4_create(lpm_context* ctx, lpm_bve_rk4** out, int64_t nverts,
 
 int lpm_bve_rk4_destroy(lpm_bve_rk4* st) {
   if (!st) return LPM_OK;
+  lpm::DeviceGuard device_guard(st->ctx->device);
   st->free_all();
   delete st;
   return LPM_OK;
@@ -411,7 +415,7 @@ int lpm_bve_rk4_advance_timestep(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
     if ((st->nv > 0 && (!vx.p || !vzeta || !vvel.p)) ||
         (st->nf > 0 && (!fx.p || !fzeta || !fvel.p || !farea || !fmask)))
       return lpm::fail(LPM_ERR_ARG, "lpm_bve_rk4_advance_timestep: null array");
-    cudaSetDevice(st->ctx->device);
+    lpm::DeviceGuard device_guard(st->ctx->device);
     st->advance(vx, vzeta, vvel, fx, fzeta, fvel, farea, fmask);
     return LPM_OK;
   } catch (...) {
@@ -428,7 +432,8 @@ int lpm_ic2d_rk2_create(lpm_context* ctx, lpm_ic2d_rk2** out, int ndim,
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: ndim must be 2 or 3");
     if (nverts < 0 || nfaces < 0 || nverts + nfaces > (int64_t(1) << 31) - 1)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: sizes out of range");
-    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
+    if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD &&
+        precision != LPM_FP64_EXACT)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: bad precision");
     if (!std::isfinite(dt) || !std::isfinite(cor) || !std::isfinite(eps) || eps < 0)
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_create: non-finite dt/cor or bad eps");
@@ -456,6 +461,7 @@ int lpm_ic2d_rk2_create(lpm_context* ctx, lpm_ic2d_rk2** out, int ndim,
 
 int lpm_ic2d_rk2_destroy(lpm_ic2d_rk2* st) {
   if (!st) return LPM_OK;
+  lpm::DeviceGuard device_guard(st->ctx->device);
   st->free_all();
   delete st;
   return LPM_OK;
@@ -471,7 +477,7 @@ int lpm_ic2d_rk2_advance_timestep(lpm_ic2d_rk2* st, lpm_view vx,
     if ((st->nv > 0 && (!vx.p || !vzeta || !vvel.p)) ||
         (st->nf > 0 && (!fx.p || !fzeta || !fvel.p || !farea || !fmask)))
       return lpm::fail(LPM_ERR_ARG, "lpm_ic2d_rk2_advance_timestep: null array");
-    cudaSetDevice(st->ctx->device);
+    lpm::DeviceGuard device_guard(st->ctx->device);
     st->advance(vx, vzeta, vvel, vpsi, fx, fzeta, fvel, fpsi, farea, fmask);
     return LPM_OK;
   } catch (...) {
@@ -495,7 +501,7 @@ int lpm_bve_rk4_set_farfield(lpm_bve_rk4* st, lpm_farfield* ff, int rebuild_ever
 int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches) {
   try {
     if (!st || !ms || !launches) return lpm::fail(LPM_ERR_ARG, "null argument");
-    cudaSetDevice(st->ctx->device);
+    lpm::DeviceGuard device_guard(st->ctx->device);
     st->nbody_time(ms, launches);
     return LPM_OK;
   } catch (...) {
@@ -506,7 +512,7 @@ int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches) {
 int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches) {
   try {
     if (!st || !ms || !launches) return lpm::fail(LPM_ERR_ARG, "null argument");
-    cudaSetDevice(st->ctx->device);
+    lpm::DeviceGuard device_guard(st->ctx->device);
     st->nbody_time(ms, launches);
     return LPM_OK;
   } catch (...) {

@@ -2,7 +2,12 @@
 
 Tolerances (relative to the largest reference magnitude, the ErrNorms linf
 normalisation of src/lpm_error.hpp:81-91):
-  FP64 path   1e-12 (each pair term is bit-identical; only sum grouping differs)
+  FP64_EXACT  1e-12 on every target (each pair term is bit-identical; only
+              the grouping of the sum differs), non-finite entries matched
+  FP64        1e-12 on vertices and leaf faces (cross product out of the sum,
+              Newton-Raphson quotients); at a divided parent slot whose centre
+              coincides with its central child's, the reference's value is
+              non-finite and the hoisted form's is not defined either
   FP32C path  2e-6 velocity, 2e-6 stream function on leaf targets
 """
 import math
@@ -61,16 +66,20 @@ def sphere_case(level, seed=core.MESH_ICOS_TRI, kind=core.IC_RH54, params=None, 
 
 
 def tolerance(precision):
-    return {core.FP64: TOL64, core.FP64_CHORD: TOL64C, core.FP32C: TOL32}[precision]
+    return {core.FP64: TOL64, core.FP64_EXACT: TOL64, core.FP64_CHORD: TOL64C,
+            core.FP32C: TOL32}[precision]
+
+
+REF_FORM = (core.FP64, core.FP64_EXACT)
 
 
 @pytest.mark.parametrize("level", [0, 2, 3])
-@pytest.mark.parametrize("precision", [core.FP64, core.FP64_CHORD, core.FP32C])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP64_EXACT, core.FP64_CHORD, core.FP32C])
 def test_bve_functors(gpu_ctx, oracle, level, precision):
     ctx = gpu_ctx
     ctx.set_precision(precision)
     vx, fx, fa, fm, zf = sphere_case(level, noise=0.5)
-    oracle.set_sphere_form(precision != core.FP64)
+    oracle.set_sphere_form(precision not in REF_FORM)
     try:
         psi_v, u_v = oracle.bve_vertex_solve(vx, fx, zf, fa, fm)
         psi_f, u_f = oracle.bve_face_solve(fx, zf, fa, fm)
@@ -85,7 +94,7 @@ def test_bve_functors(gpu_ctx, oracle, level, precision):
     F.bve_face_solve(ctx, gfp, gfu, dfx, dz, da, dm)
     ctx.synchronize()
     leaf = fm == 0
-    if precision == core.FP64:
+    if precision == core.FP64_EXACT:
         assert rel(gu.cpu(), u_v) < TOL64
         assert rel(gp.cpu(), psi_v) < TOL64
         assert rel(gfu.cpu(), u_f) < TOL64
@@ -107,7 +116,7 @@ def test_bve_functors(gpu_ctx, oracle, level, precision):
     F.bve_face_stream_fn(ctx, gfp2, dfx, dz, da, dm)
     ctx.synchronize()
     assert same(gu2, gu) and same(gfu2, gfu)
-    tolp = 0 if precision == core.FP64 else 1e-12
+    tolp = 0 if precision in REF_FORM else 1e-12
     assert rel(gp2.cpu(), gp.cpu()) <= tolp and rel(gfp2.cpu(), gfp.cpu()) <= tolp
 
 
@@ -132,7 +141,7 @@ def test_bve_soa_layout(gpu_ctx, oracle):
 
 
 @pytest.mark.parametrize("eps", [0.0, 0.05])
-@pytest.mark.parametrize("precision", [core.FP64, core.FP64_CHORD, core.FP32C])
+@pytest.mark.parametrize("precision", [core.FP64, core.FP64_EXACT, core.FP64_CHORD, core.FP32C])
 @pytest.mark.parametrize("geom", ["sphere", "plane"])
 def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
     ctx = gpu_ctx
@@ -145,7 +154,7 @@ def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
         vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 4, 4.0)
         zf = core.eval_ic(core.IC_DIPOLE_PAIR, (2.0, 1.0, -2.0, 0.0, -2.0, 1.0, 2.0, 0.0), fx)
     nd = vx.shape[1]
-    oracle.set_sphere_form(precision != core.FP64)
+    oracle.set_sphere_form(precision not in REF_FORM)
     try:
         u_p, psi_p = oracle.ic2d_passive_sums(vx, fx, zf, fa, fm, eps)
         u_a, psi_a = oracle.ic2d_active_sums(fx, zf, fa, fm, eps)
@@ -163,7 +172,7 @@ def test_ic2d_functors(gpu_ctx, oracle, eps, precision, geom):
     tol = tolerance(precision)
     assert rel(gu.cpu(), u_p) < tol
     assert rel(gp.cpu(), psi_p) < tol
-    sel = slice(None) if precision == core.FP64 else leaf
+    sel = slice(None) if precision == core.FP64_EXACT else leaf
     assert rel(fu.cpu().numpy()[sel], u_a[sel]) < tol
     assert rel(fp.cpu().numpy()[sel], psi_a[sel]) < tol
 
@@ -314,3 +323,33 @@ def test_one_call_direct_sums(gpu_ctx, precision):
     stream.synchronize()
     assert torch.equal(u3, u1) and torch.equal(p3, p1)
     check(lib().lpm_one_call_release())
+
+
+@pytest.mark.parametrize("level", [4, 5])
+@pytest.mark.parametrize("eps", [0.0, 0.01])
+def test_fp64_hoisted_vs_exact(gpu_ctx, level, eps):
+    """LPM_FP64 (hoisted cross product, Newton-Raphson quotients) against
+    LPM_FP64_EXACT (the reference's term-by-term arithmetic) on vertices and
+    leaf faces: within 1e-12, and the two share their inputs exactly."""
+    ctx = gpu_ctx
+    vx, fx, fa, fm, zf = sphere_case(level, noise=0.5)
+    T = [dev(a) for a in (vx, fx, zf, fa, fm)]
+    out = {}
+    for prec in (core.FP64, core.FP64_EXACT):
+        ctx.set_precision(prec)
+        vu = torch.zeros(vx.shape[0], 3, dtype=torch.float64, device="cuda")
+        vp = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
+        fu = torch.zeros(fx.shape[0], 3, dtype=torch.float64, device="cuda")
+        fp = torch.zeros(fx.shape[0], dtype=torch.float64, device="cuda")
+        if eps == 0.0:
+            F.bve_vertex_solve(ctx, vp, vu, T[0], T[1], T[2], T[3], T[4])
+            F.bve_face_solve(ctx, fp, fu, T[1], T[2], T[3], T[4])
+        else:
+            F.ic2d_passive_sums(ctx, vu, vp, T[0], T[1], T[2], T[3], T[4], eps)
+            F.ic2d_active_sums(ctx, fu, fp, T[1], T[2], T[3], T[4], eps, self_rule=1)
+        ctx.synchronize()
+        out[prec] = [a.cpu().numpy() for a in (vu, vp, fu, fp)]
+    leaf = fm == 0
+    a, b = out[core.FP64], out[core.FP64_EXACT]
+    assert rel(a[0], b[0]) < TOL64 and rel(a[1], b[1]) < TOL64
+    assert rel(a[2][leaf], b[2][leaf]) < TOL64 and rel(a[3][leaf], b[3][leaf]) < TOL64
