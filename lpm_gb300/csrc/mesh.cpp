@@ -13,10 +13,19 @@
 // a divided quad's centre becomes a vertex (src/mesh/lpm_faces_impl.hpp
 // :503-517).
 //
-// The seeds are built here from their geometry (icosahedron, cube, 2x2
-// square), not read from the reference's seed files, so vertex numbering may
-// differ from the reference's; the point sets, areas and the parent/leaf slot
-// structure are the same.
+// Seeds.  The reference reads its seeds from mesh_seeds/*.dat
+// (MeshSeed::read_file, src/mesh/lpm_mesh_seed.cpp:20-201): vertex
+// coordinates, face centres, face vertex lists.  The three seeds of the
+// direct-sum path are generated here in the same numbering and with the same
+// values bit for bit: the icosahedron's coordinates are the correctly rounded
+// values of their closed forms ((5 +- sqrt5)/10, sqrt((5 +- sqrt5)/10),
+// 2/sqrt5, 1/sqrt5, evaluated in double-double arithmetic and rounded once)
+// and its face centres the seed files' rule c = ((v0 + v1) + v2) / 3,
+// c / sqrt((c0^2 + c1^2) + c2^2); the cube's vertices are +-1/sqrt(3) with the
+// face centres on the axes; the square's are the 3 x 3 grid of [-1, 1]^2
+// scaled by the radius.  A face's edge i joins its vertices i and i + 1 in
+// every seed, so dividing edges in face order numbers the new vertices as
+// the reference's edge-based dividers do.
 
 #include <array>
 #include <cmath>
@@ -101,15 +110,21 @@ struct Builder {
     return ar;
   }
 
-  void add_face(const int64_t* vs) {
+  // a face with the given centre; its area about that centre
+  // (MeshSeed::face_area, src/mesh/lpm_mesh_seed.cpp:281-295)
+  void add_face_at(const double* c, const int64_t* vs) {
     std::array<int64_t, 4> f{-1, -1, -1, -1};
     for (int i = 0; i < nfv; ++i) f[i] = vs[i];
-    double c[3] = {0, 0, 0};
-    barycenter(c, vs, nfv);
     for (int k = 0; k < ndim; ++k) fx.push_back(c[k]);
     area.push_back(polygon_area(c, vs, nfv));
     mask.push_back(0);
     fverts.push_back(f);
+  }
+  // a child face: centre at the barycentre of its vertices
+  void add_face(const int64_t* vs) {
+    double c[3] = {0, 0, 0};
+    barycenter(c, vs, nfv);
+    add_face_at(c, vs);
   }
 
   int64_t edge_mid(int64_t a, int64_t b) {
@@ -168,107 +183,128 @@ struct Builder {
     }
   }
 
-  // Orient a face counter-clockwise as seen from outside (sphere) or from +z.
-  void orient(int64_t* vs) const {
-    const double* a = v(vs[0]);
-    const double* b = v(vs[1]);
-    const double* c = v(vs[2]);
-    double s;
-    if (sphere) {
-      const double ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
-      const double ac[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
-      const double n[3] = {ab[1] * ac[2] - ab[2] * ac[1],
-                           ab[2] * ac[0] - ab[0] * ac[2],
-                           ab[0] * ac[1] - ab[1] * ac[0]};
-      s = n[0] * (a[0] + b[0] + c[0]) + n[1] * (a[1] + b[1] + c[1]) +
-          n[2] * (a[2] + b[2] + c[2]);
-    } else {
-      s = (b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0]);
-    }
-    if (s < 0) {
-      // reverse, keeping vs[0]
-      for (int i = 1, j = nfv - 1; i < j; ++i, --j) std::swap(vs[i], vs[j]);
-    }
-  }
 };
 
+// ---- double-double arithmetic for the icosahedron's coordinates ---------
+struct DD {
+  double hi, lo;
+};
+DD quick_two_sum(double a, double b) {
+  const double s = a + b;
+  return {s, b - (s - a)};
+}
+DD two_sum(double a, double b) {
+  const double s = a + b;
+  const double bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+DD dd_add(DD a, DD b) {
+  DD s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+DD dd_neg(DD a) { return {-a.hi, -a.lo}; }
+// a / b for a double-double a and a double b: quotient plus the exact residual
+DD dd_div(DD a, double b) {
+  const double q = a.hi / b;
+  const double p = q * b;
+  const double pe = std::fma(q, b, -p);
+  const double r = ((a.hi - p) - pe) + a.lo;
+  return quick_two_sum(q, r / b);
+}
+// b / a for a double b and a double-double a
+DD dd_rdiv(double b, DD a) {
+  const double q = b / a.hi;
+  const double p = q * a.hi;
+  const double pe = std::fma(q, a.hi, -p);
+  const double r = ((b - p) - pe) - q * a.lo;
+  return quick_two_sum(q, r / a.hi);
+}
+DD dd_sqrt(DD a) {
+  const double x = std::sqrt(a.hi);
+  const double p = x * x;
+  const double pe = std::fma(x, x, -p);
+  const double r = ((a.hi - p) - pe) + a.lo;
+  return quick_two_sum(x, r / (2.0 * x));
+}
+double dd_round(DD a) { return a.hi + a.lo; }
+
+// IcosTriSphereSeed: vertex 0 the north pole, 1-5 the upper ring at
+// longitudes 36 + 72 k degrees, 6-10 the lower ring at 72 k degrees, 11 the
+// south pole; faces: the five around the north pole, then for each k the
+// band faces (U(k), L(k), L(k+1)) and (L(k+1), U(k+1), U(k)), then the five
+// around the south pole.
 void seed_icosahedron(Builder& b) {
   b.ndim = 3;
   b.sphere = true;
   b.nfv = 3;
-  const double zr = 1.0 / std::sqrt(5.0), rr = 2.0 / std::sqrt(5.0);
-  const double north[3] = {0, 0, 1};
-  b.add_vertex(north);
-  for (int k = 0; k < 5; ++k) {  // upper ring 1..5
-    const double t = 2 * PI * k / 5;
-    const double p[3] = {rr * std::cos(t), rr * std::sin(t), zr};
-    b.add_vertex(p);
-  }
-  for (int k = 0; k < 5; ++k) {  // lower ring 6..10
-    const double t = 2 * PI * k / 5 + PI / 5;
-    const double p[3] = {rr * std::cos(t), rr * std::sin(t), -zr};
-    b.add_vertex(p);
-  }
-  const double south[3] = {0, 0, -1};
-  b.add_vertex(south);
+  const DD s5 = dd_sqrt(DD{5.0, 0.0});
+  const DD ap = dd_div(dd_add(DD{5.0, 0.0}, s5), 10.0);          // (5 + sqrt5)/10
+  const DD am = dd_div(dd_add(DD{5.0, 0.0}, dd_neg(s5)), 10.0);  // (5 - sqrt5)/10
+  const double A = dd_round(ap);            // r cos 36
+  const double Bm = dd_round(dd_sqrt(am));  // r sin 36
+  const double C = dd_round(am);            // r cos 72
+  const double D = dd_round(dd_sqrt(ap));   // r sin 72
+  const double E = dd_round(dd_rdiv(2.0, s5));  // r = 2/sqrt5
+  const double Z = dd_round(dd_rdiv(1.0, s5));  // z = 1/sqrt5
+  const double v[12][3] = {{0, 0, 1},   {A, Bm, Z},   {-C, D, Z},   {-E, 0, Z},
+                           {-C, -D, Z}, {A, -Bm, Z},  {E, 0, -Z},   {C, D, -Z},
+                           {-A, Bm, -Z}, {-A, -Bm, -Z}, {C, -D, -Z}, {0, 0, -1}};
+  for (int i = 0; i < 12; ++i) b.add_vertex(v[i]);
   auto U = [](int k) { return int64_t(1 + (k % 5)); };
   auto L = [](int k) { return int64_t(6 + (k % 5)); };
+  std::vector<std::array<int64_t, 3>> f;
+  for (int k = 0; k < 5; ++k) f.push_back({0, U(k), U(k + 1)});
   for (int k = 0; k < 5; ++k) {
-    int64_t f[3] = {0, U(k), U(k + 1)};
-    b.orient(f);
-    b.add_face(f);
+    f.push_back({U(k), L(k), L(k + 1)});
+    f.push_back({L(k + 1), U(k + 1), U(k)});
   }
-  for (int k = 0; k < 5; ++k) {
-    int64_t f1[3] = {U(k), L(k), U(k + 1)};
-    b.orient(f1);
-    b.add_face(f1);
-    int64_t f2[3] = {U(k + 1), L(k), L(k + 1)};
-    b.orient(f2);
-    b.add_face(f2);
-  }
-  for (int k = 0; k < 5; ++k) {
-    int64_t f[3] = {11, L(k + 1), L(k)};
-    b.orient(f);
-    b.add_face(f);
+  for (int k = 0; k < 5; ++k) f.push_back({11, L(k + 1), L(k)});
+  for (const auto& t : f) {
+    double c[3];
+    for (int k = 0; k < 3; ++k) c[k] = ((b.v(t[0])[k] + b.v(t[1])[k]) + b.v(t[2])[k]) / 3.0;
+    const double n = std::sqrt((c[0] * c[0] + c[1] * c[1]) + c[2] * c[2]);
+    for (int k = 0; k < 3; ++k) c[k] /= n;
+    b.add_face_at(c, t.data());
   }
 }
 
+// CubedSphereSeed: vertices (s,-s,s), (s,-s,-s), (s,s,-s), (s,s,s),
+// (-s,s,-s), (-s,s,s), (-s,-s,-s), (-s,-s,s) with s = 1/sqrt3; faces
+// +x, +y, -x, -y, +z, -z with their centres on the axes.
 void seed_cube(Builder& b) {
   b.ndim = 3;
   b.sphere = true;
   b.nfv = 4;
   const double s = 1.0 / std::sqrt(3.0);
-  // vertex index = 4*(x>0) + 2*(y>0) + (z>0)
-  for (int i = 0; i < 8; ++i) {
-    const double p[3] = {(i & 4) ? s : -s, (i & 2) ? s : -s, (i & 1) ? s : -s};
-    b.add_vertex(p);
-  }
-  const int64_t faces[6][4] = {{4, 6, 7, 5}, {0, 1, 3, 2}, {2, 3, 7, 6},
-                               {0, 4, 5, 1}, {1, 5, 7, 3}, {0, 2, 6, 4}};
-  for (int f = 0; f < 6; ++f) {
-    int64_t vs[4] = {faces[f][0], faces[f][1], faces[f][2], faces[f][3]};
-    b.orient(vs);
-    b.add_face(vs);
-  }
+  const double v[8][3] = {{s, -s, s},  {s, -s, -s}, {s, s, -s},  {s, s, s},
+                          {-s, s, -s}, {-s, s, s},  {-s, -s, -s}, {-s, -s, s}};
+  for (int i = 0; i < 8; ++i) b.add_vertex(v[i]);
+  const int64_t faces[6][4] = {{0, 1, 2, 3}, {3, 2, 4, 5}, {5, 4, 6, 7},
+                               {7, 6, 1, 0}, {7, 0, 3, 5}, {1, 6, 4, 2}};
+  const double ctr[6][3] = {{1, 0, 0}, {0, 1, 0}, {-1, 0, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  for (int f = 0; f < 6; ++f) b.add_face_at(ctr[f], faces[f]);
 }
 
+// QuadRectSeed on [-r, r]^2: the boundary vertices counter-clockwise from
+// (-r, r) down the left side, then the centre; four faces with centres
+// (+-r/2, +-r/2).
 void seed_square(Builder& b, double radius) {
   b.ndim = 2;
   b.sphere = false;
   b.nfv = 4;
-  // 3 x 3 grid on [-r, r]^2, index = 3*row + col, row along y
-  for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) {
-      const double p[2] = {radius * (c - 1), radius * (r - 1)};
-      b.add_vertex(p);
-    }
-  for (int r = 0; r < 2; ++r)
-    for (int c = 0; c < 2; ++c) {
-      int64_t vs[4] = {3 * r + c, 3 * r + c + 1, 3 * (r + 1) + c + 1,
-                       3 * (r + 1) + c};
-      b.orient(vs);
-      b.add_face(vs);
-    }
+  const double v[9][2] = {{-1, 1}, {-1, 0}, {-1, -1}, {0, -1}, {1, -1},
+                          {1, 0},  {1, 1},  {0, 1},   {0, 0}};
+  for (int i = 0; i < 9; ++i) {
+    const double p[2] = {v[i][0] * radius, v[i][1] * radius};
+    b.add_vertex(p);
+  }
+  const int64_t faces[4][4] = {{0, 1, 8, 7}, {1, 2, 3, 8}, {8, 3, 4, 5}, {7, 8, 5, 6}};
+  const double ctr[4][2] = {{-0.5, 0.5}, {-0.5, -0.5}, {0.5, -0.5}, {0.5, 0.5}};
+  for (int f = 0; f < 4; ++f) {
+    const double c[2] = {ctr[f][0] * radius, ctr[f][1] * radius};
+    b.add_face_at(c, faces[f]);
+  }
 }
 
 int64_t ipow4(int l) {

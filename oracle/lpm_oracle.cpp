@@ -104,24 +104,26 @@ inline void biot_savart(double* u, const double* tgt, const double* src,
 
 // Incompressible2DKernels<SphereGeometry>::kernel_vals,
 // src/lpm_incompressible2d_kernels.hpp:35-47.
+// want_psi = false skips the stream function's log (the velocity terms are
+// the same either way; the reference always computes both).
 inline void sphere_kernel_vals(double* r, const double* x, const double* y,
-                               double eps) {
+                               double eps, bool want_psi = true) {
   const double arg = one_minus_dot(x, y) + eps * eps;
   scross(r, x, y);
   for (int k = 0; k < 3; ++k) r[k] /= (-4 * PI * arg);
-  r[3] = -std::log(arg) / (4 * PI);
+  r[3] = want_psi ? -std::log(arg) / (4 * PI) : 0.0;
 }
 
 // Incompressible2DKernels<PlaneGeometry>::kernel_vals,
 // src/lpm_incompressible2d_kernels.hpp:72-84.
 inline void plane_kernel_vals(double* r, const double* x, const double* y,
-                              double eps) {
+                              double eps, bool want_psi = true) {
   const double xmy[2] = {x[0] - y[0], x[1] - y[1]};
   const double arg = (xmy[0] * xmy[0] + xmy[1] * xmy[1]) + eps * eps;
   const double denom = 2 * PI * arg;
   r[0] = -xmy[1] / denom;
   r[1] = xmy[0] / denom;
-  r[2] = -std::log(arg) / (4 * PI);
+  r[2] = want_psi ? -std::log(arg) / (4 * PI) : 0.0;
 }
 
 int g_threads = 0;
@@ -177,9 +179,9 @@ inline void ic2d_target(int ndim, double* u, double* psi, const double* x,
     const double gamma = zeta[j] * area[j];
     double r[4];
     if (ndim == 3)
-      sphere_kernel_vals(r, x, y + 3 * j, eps);
+      sphere_kernel_vals(r, x, y + 3 * j, eps, psi != nullptr);
     else
-      plane_kernel_vals(r, x, y + 2 * j, eps);
+      plane_kernel_vals(r, x, y + 2 * j, eps, psi != nullptr);
     for (int k = 0; k < nvals; ++k) a[k].add(r[k] * gamma);
   }
   if (u)

@@ -14,8 +14,11 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "build" / "liblpm_oracle.so"
+LIB_NATIVE = HERE / "build" / "liblpm_oracle_native.so"
 
 _lib = None
+_lib_native = None
+_use_native = False
 
 
 def build() -> Path:
@@ -25,35 +28,54 @@ def build() -> Path:
     return LIB
 
 
+def use_native(on: bool) -> None:
+    """Route the calls below to the build tuned for this CPU (timing only)."""
+    global _use_native
+    _use_native = bool(on)
+
+
 def lib() -> C.CDLL:
-    global _lib
+    global _lib, _lib_native
+    if _use_native:
+        if _lib_native is None:
+            _lib_native = _load(LIB_NATIVE)
+        return _lib_native
     if _lib is None:
-        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "lpm_oracle.cpp").stat().st_mtime:
-            build()
-        L = C.CDLL(str(LIB))
-        vp, l, i, d = C.c_void_p, C.c_long, C.c_int, C.c_double
-        sig = {
-            "oracle_set_threads": [i],
-            "oracle_swe_plane_sums": [l, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, i, vp],
-            "oracle_swe_sphere_sums": [l, vp, l, vp, vp, vp, vp, vp, d, i, vp],
-            "oracle_set_sphere_form": [i],
-            "oracle_max_threads": [],
-            "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
-            "oracle_bve_face_solve": [vp, vp, l, vp, vp, vp, vp, vp, l, i],
-            "oracle_ic2d_passive_sums": [i, vp, vp, vp, l, vp, vp, vp, vp, vp, d, l, i],
-            "oracle_ic2d_active_sums": [i, vp, vp, l, vp, vp, vp, vp, vp, d, l, i, i],
-            "oracle_bve_rk4_step": [l, vp, vp, vp, l, vp, vp, vp, vp, vp, d, d, d, i, i],
-            "oracle_ic2d_init_direct_sums": [i, l, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, i],
-            "oracle_ic2d_rk2_step": [i, l, vp, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, d, i],
-            "oracle_invariants": [i, l, vp, vp, vp, vp, vp],
-            "oracle_err_norms": [i, l, vp, vp, vp, vp, vp],
-        }
-        for k, a in sig.items():
-            f = getattr(L, k)
-            f.argtypes = a
-            f.restype = C.c_int if k == "oracle_max_threads" else None
-        _lib = L
+        _lib = _load(LIB)
     return _lib
+
+
+def _load(path: Path) -> C.CDLL:
+    srcs = [HERE / "lpm_oracle.cpp", HERE / "lpm_oracle_mesh.cpp", HERE / "Makefile"]
+    if not path.exists() or path.stat().st_mtime < max(p.stat().st_mtime for p in srcs):
+        build()
+    L = C.CDLL(str(path))
+    vp, l, i, d = C.c_void_p, C.c_long, C.c_int, C.c_double
+    sig = {
+        "oracle_set_threads": [i],
+        "oracle_swe_plane_sums": [l, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, i, vp],
+        "oracle_swe_sphere_sums": [l, vp, l, vp, vp, vp, vp, vp, d, i, vp],
+        "oracle_set_sphere_form": [i],
+        "oracle_max_threads": [],
+        "oracle_bve_vertex_solve": [vp, vp, vp, l, vp, vp, vp, vp, vp, l, i],
+        "oracle_bve_face_solve": [vp, vp, l, vp, vp, vp, vp, vp, l, i],
+        "oracle_ic2d_passive_sums": [i, vp, vp, vp, l, vp, vp, vp, vp, vp, d, l, i],
+        "oracle_ic2d_active_sums": [i, vp, vp, l, vp, vp, vp, vp, vp, d, l, i, i],
+        "oracle_bve_rk4_step": [l, vp, vp, vp, l, vp, vp, vp, vp, vp, d, d, d, i, i],
+        "oracle_ic2d_init_direct_sums": [i, l, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, i],
+        "oracle_ic2d_rk2_step": [i, l, vp, vp, vp, vp, l, vp, vp, vp, vp, vp, vp, d, d, d, i],
+        "oracle_invariants": [i, l, vp, vp, vp, vp, vp],
+        "oracle_err_norms": [i, l, vp, vp, vp, vp, vp],
+        "oracle_mesh_build": [i, i, i, l, l, l, vp, vp, vp, vp, d, i, l, l, vp, vp, vp, vp,
+                              vp],
+        "oracle_ic_eval": [i, vp, i, i, l, vp, vp],
+    }
+    ret_int = ("oracle_max_threads", "oracle_mesh_build", "oracle_ic_eval")
+    for k, a in sig.items():
+        f = getattr(L, k)
+        f.argtypes = a
+        f.restype = C.c_int if k in ret_int else None
+    return L
 
 
 def _p(a):
@@ -117,13 +139,16 @@ def bve_face_solve(fx, zeta, area, mask, want_u=True, want_psi=True, tgt_idx=Non
     return psi, u
 
 
-def ic2d_passive_sums(x, y, zeta, area, mask, eps, tgt_idx=None, compensated=False):
+def ic2d_passive_sums(x, y, zeta, area, mask, eps, tgt_idx=None, compensated=False,
+                      want_psi=True):
+    """Incompressible2DPassiveSums: (u, psi); want_psi=False skips the
+    stream function (psi is returned as None)."""
     x, y, zeta, area = _f(x), _f(y), _f(zeta), _f(area)
     ndim = x.shape[1]
     mask = np.ascontiguousarray(mask, np.uint8)
     idx = None if tgt_idx is None else np.ascontiguousarray(tgt_idx, np.int64)
     n = x.shape[0] if idx is None else idx.shape[0]
-    u, psi = np.zeros((n, ndim)), np.zeros(n)
+    u, psi = np.zeros((n, ndim)), (np.zeros(n) if want_psi else None)
     lib().oracle_ic2d_passive_sums(ndim, _p(u), _p(psi), _p(x), n, _p(idx), _p(y), _p(zeta),
                                    _p(area), _p(mask), float(eps), y.shape[0], int(compensated))
     return u, psi
@@ -240,3 +265,75 @@ def err_norms(appx, exact, wt=None, mask=None):
     out = np.zeros(3)
     lib().oracle_err_norms(a.shape[1], a.shape[0], _p(a), _p(e), _p(w), _p(m), _p(out))
     return tuple(out)
+
+
+# ---- inputs: the reference's meshes and initial conditions -----------------
+# Mesh kinds and initial-condition kinds (the same numbers as the library's
+# LPM_MESH_* / LPM_IC_* constants).
+MESH_ICOS_TRI, MESH_CUBED_SPHERE, MESH_QUAD_RECT = 1, 2, 3
+IC_SOLID_BODY, IC_GAUSSIAN_SPHERE, IC_RH54, IC_DIPOLE_PAIR, IC_MULTI_GAUSSIAN = 1, 2, 3, 4, 5
+
+# The reference's seed files, parsed by tests/golden/make_mesh_seeds.py.
+SEED_FILE = HERE.parent / "tests" / "golden" / "mesh_seeds.npz"
+_SEEDS = {MESH_ICOS_TRI: ("icos", 3, True), MESH_CUBED_SPHERE: ("cubed", 3, True),
+          MESH_QUAD_RECT: ("quad", 2, False)}
+_seed_cache = {}
+
+
+def seed(kind):
+    """(coordinates, edges, face vertices, face edges) of a reference seed."""
+    if kind not in _seed_cache:
+        name = _SEEDS[kind][0]
+        with np.load(SEED_FILE) as z:
+            _seed_cache[kind] = tuple(np.ascontiguousarray(z[f"{name}_{t}"]) for t in
+                                      ("crds", "edges", "faceverts", "faceedges"))
+    return _seed_cache[kind]
+
+
+def mesh_sizes(kind, level):
+    """(vertices, face slots) of a uniform mesh: n_vertices_at_tree_level and
+    the sum of n_faces_at_tree_level over levels (src/mesh/lpm_mesh_seed.cpp:306-371)."""
+    if kind == MESH_ICOS_TRI:
+        return 2 + 10 * 4 ** level, sum(20 * 4 ** i for i in range(level + 1))
+    if kind == MESH_CUBED_SPHERE:
+        return 2 + 6 * 4 ** level, sum(6 * 4 ** i for i in range(level + 1))
+    side = 3 + sum(2 ** i for i in range(1, level + 1))
+    return side * side, sum(4 * 4 ** i for i in range(level + 1))
+
+
+def mesh_build(kind, level, radius=1.0):
+    """The reference's uniform mesh (tree_init from its seed file): vertex
+    coordinates, face centres (all tree levels), areas, masks and face vertex
+    lists."""
+    crds, edges, fverts, fedges = seed(kind)
+    ndim, sphere = _SEEDS[kind][1], _SEEDS[kind][2]
+    nfv = fverts.shape[1]
+    nv, nf = mesh_sizes(kind, level)
+    vx, fx = np.zeros((nv, ndim)), np.zeros((nf, ndim))
+    fa, fm = np.zeros(nf), np.zeros(nf, np.uint8)
+    fv = np.zeros((nf, nfv), np.int64)
+    nverts0 = crds.shape[0] - fverts.shape[0]  # seed rows: vertices, then face centres
+    rc = lib().oracle_mesh_build(ndim, int(sphere), nfv, nverts0, edges.shape[0], fverts.shape[0],
+                                 _p(_f(crds)), _p(edges), _p(fverts), _p(fedges), float(radius),
+                                 int(level), nv, nf, _p(vx), _p(fx), _p(fa), _p(fm), _p(fv))
+    if rc != 0:
+        raise RuntimeError("oracle_mesh_build: size mismatch")
+    return vx, fx, fa, fm, fv
+
+
+def ic_eval(kind, params, x):
+    """Initial relative vorticity at the rows of x (see oracle_ic_eval)."""
+    x = _f(x)
+    prm = np.ascontiguousarray(params, np.float64)
+    out = np.zeros(x.shape[0])
+    rc = lib().oracle_ic_eval(int(kind), _p(prm), prm.size, x.shape[1], x.shape[0], _p(x),
+                              _p(out))
+    if rc != 0:
+        raise ValueError("oracle_ic_eval: unknown kind or too few parameters")
+    return out
+
+
+def mesh(kind, level, radius=1.0):
+    """(vertices, face centres, areas, masks) of the reference's uniform mesh."""
+    vx, fx, fa, fm, _ = mesh_build(kind, level, radius)
+    return vx, fx, fa, fm

@@ -3,9 +3,12 @@
     python tests/golden/make_golden.py
 
 The reference itself cannot be built here (it needs Kokkos and friends), so
-the fixtures hold the oracle's outputs on small seeded inputs.  They freeze
-the oracle (checked on CPU on every platform) and give the CUDA path a fixed
-target independent of the live oracle.
+the fixtures hold the oracle's outputs on small seeded inputs: the
+reference's own meshes (grown by the oracle's restatement of tree_init from
+the reference's seed files, tests/golden/mesh_seeds.npz) and initial
+conditions restated by the oracle, so no product code is involved.  They
+freeze the oracle (checked on CPU on every platform) and give the CUDA path a
+fixed target independent of the live oracle.
 """
 import math
 import sys
@@ -19,17 +22,16 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 
 import lpm_oracle as O  # noqa: E402
-from lpm_gb300 import core  # noqa: E402
 
 OMEGA = 2 * math.pi
 
 
 def bve_case():
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     w = OMEGA / 12.5
-    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    fz = O.ic_eval(O.IC_RH54, (w, -w), fx)
     fz = fz + 0.25 * np.random.default_rng(11).standard_normal(fz.shape)
-    vz = core.eval_ic(core.IC_RH54, (w, -w), vx)
+    vz = O.ic_eval(O.IC_RH54, (w, -w), vx)
     vpsi, vu = O.bve_vertex_solve(vx, fx, fz, fa, fm)
     fpsi, fu = O.bve_face_solve(fx, fz, fa, fm)
     s = O.BVEState(vx, vz, vu, fx, fz, fu, fa, fm)
@@ -42,9 +44,9 @@ def bve_case():
 
 
 def ic2d_sphere_case():
-    vx, fx, fa, fm = core.build_mesh(core.MESH_CUBED_SPHERE, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_CUBED_SPHERE, 2, 1.0)
     prm = (4 * math.pi, 4.0, 0.0, math.pi / 20, 0.0, 0.0)
-    fz = core.eval_ic(core.IC_GAUSSIAN_SPHERE, prm, fx)
+    fz = O.ic_eval(O.IC_GAUSSIAN_SPHERE, prm, fx)
     out = {}
     for eps in (0.0, 0.05):
         up, pp = O.ic2d_passive_sums(vx, fx, fz, fa, fm, eps)
@@ -55,10 +57,10 @@ def ic2d_sphere_case():
 
 
 def ic2d_plane_case():
-    vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 3, 4.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_QUAD_RECT, 3, 4.0)
     prm = (2.0, 1.0, -2.0, 0.0, -2.0, 1.0, 2.0, 0.0)
-    fz = core.eval_ic(core.IC_DIPOLE_PAIR, prm, fx)
-    vz = core.eval_ic(core.IC_DIPOLE_PAIR, prm, vx)
+    fz = O.ic_eval(O.IC_DIPOLE_PAIR, prm, fx)
+    vz = O.ic_eval(O.IC_DIPOLE_PAIR, prm, vx)
     up, pp = O.ic2d_passive_sums(vx, fx, fz, fa, fm, 0.02)
     ua, pa = O.ic2d_active_sums(fx, fz, fa, fm, 0.02)
     s = O.IC2DState(vx, vz, fx, fz, fa, fm, 0.02, 0.0)

@@ -16,14 +16,14 @@ import math
 import numpy as np
 import pytest
 
-from lpm_gb300 import core
+import lpm_oracle as O
 
 OMEGA = 2 * math.pi
 
 
 def solid_body(level):
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
-    zf = core.eval_ic(core.IC_SOLID_BODY, (), fx)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, level, 1.0)
+    zf = O.ic_eval(O.IC_SOLID_BODY, (), fx)
     return vx, fx, fa, fm, zf
 
 
@@ -46,8 +46,8 @@ def test_rossby_haurwitz_velocity(oracle):
     w = OMEGA / 12.5
     errs = []
     for level in (3, 4):
-        vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
-        zf = core.eval_ic(core.IC_RH54, (w, -w), fx)
+        vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, level, 1.0)
+        zf = O.ic_eval(O.IC_RH54, (w, -w), fx)
         _, u = oracle.bve_vertex_solve(vx, fx, zf, fa, fm, want_psi=False)
         lat, lon = np.arcsin(vx[:, 2]), np.arctan2(vx[:, 1], vx[:, 0])
         amp, u0 = -w, w
@@ -70,7 +70,7 @@ def test_tangency(oracle):
 def test_masked_and_self_rules(oracle):
     """Masked slots never contribute; collocated BVE skips i == j; the ic2d
     active sums keep the self term for eps > 0 (psi gets -log(eps^2)/4pi Gamma_i)."""
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     zf = np.random.default_rng(2).standard_normal(fx.shape[0])
     psi_a, u_a = oracle.bve_face_solve(fx, zf, fa, fm)
     zf2 = zf.copy()
@@ -89,10 +89,10 @@ def test_masked_and_self_rules(oracle):
 
 def test_ic2d_rk2_time_convergence(oracle):
     """tests/lpm_ic2d_tests.cpp:165-188 on the oracle: rate > 1.95."""
-    vx, fx, fa, fm = core.build_mesh(core.MESH_CUBED_SPHERE, 4, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_CUBED_SPHERE, 4, 1.0)
     params = (4 * math.pi, 4.0, 0.0, math.pi / 20, 0.0, 0.0)  # GaussianVortexSphere()
-    vz, fz = core.eval_ic(core.IC_GAUSSIAN_SPHERE, params, vx), core.eval_ic(
-        core.IC_GAUSSIAN_SPHERE, params, fx)
+    vz, fz = O.ic_eval(O.IC_GAUSSIAN_SPHERE, params, vx), O.ic_eval(
+        O.IC_GAUSSIAN_SPHERE, params, fx)
     tf, nsteps = 0.5, (15, 30, 60)
 
     def run(n):
@@ -114,10 +114,10 @@ def test_ic2d_rk2_time_convergence(oracle):
 
 
 def test_bve_rk4_fourth_order(oracle):
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     w = OMEGA / 12.5
-    vz = core.eval_ic(core.IC_RH54, (w, -w), vx)
-    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    vz = O.ic_eval(O.IC_RH54, (w, -w), vx)
+    fz = O.ic_eval(O.IC_RH54, (w, -w), fx)
     _, vu = oracle.bve_vertex_solve(vx, fx, fz, fa, fm, want_psi=False)
     _, fu = oracle.bve_face_solve(fx, fz, fa, fm, want_psi=False)
     leaf = fm == 0
@@ -135,7 +135,7 @@ def test_bve_rk4_fourth_order(oracle):
 
 
 def test_facevort3_quirk_changes_only_faces(oracle):
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     fz = np.random.default_rng(4).standard_normal(fx.shape[0])
     vz = np.zeros(vx.shape[0])
     _, vu = oracle.bve_vertex_solve(vx, fx, fz, fa, fm, want_psi=False)
@@ -163,7 +163,7 @@ def test_err_norms_definition(oracle):
 
 
 def test_invariants_definition(oracle):
-    vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 2, 4.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_QUAD_RECT, 2, 4.0)
     rng = np.random.default_rng(6)
     z, u = rng.standard_normal(fx.shape[0]), rng.standard_normal((fx.shape[0], 2))
     tv, te, tk = oracle.invariants(z, u, fa, fm)

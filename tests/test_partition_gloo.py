@@ -28,16 +28,16 @@ def _worker(rank, world, port, out_dir):
     import torch.distributed as dist
 
     import lpm_oracle
-    from lpm_gb300 import core
+    import lpm_oracle as O
     from lpm_gb300.partition import problem_assignment, target_slice
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     lpm_oracle.set_threads(1)
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     w = 2 * math.pi / 12.5
-    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    fz = O.ic_eval(O.IC_RH54, (w, -w), fx)
     sl = target_slice(vx.shape[0], world, rank)
     idx = np.arange(vx.shape[0])[sl]
     _, u = lpm_oracle.bve_vertex_solve(vx, fx, fz, fa, fm, want_psi=False, tgt_idx=idx)
@@ -52,12 +52,12 @@ def _worker(rank, world, port, out_dir):
                                - target_slice(vx.shape[0], world, r).start] for r in range(world)])
     # ensemble: problems sharded longest-first, no exchange needed
     levels = [0, 1, 2, 1, 0]
-    costs = [core.mesh_sizes(core.MESH_ICOS_TRI, l)[1] ** 2 for l in levels]
+    costs = [O.mesh_sizes(O.MESH_ICOS_TRI, l)[1] ** 2 for l in levels]
     mine_p = problem_assignment(costs, world)[rank]
     sums = []
     for p in mine_p:
-        pvx, pfx, pfa, pfm = core.build_mesh(core.MESH_ICOS_TRI, levels[p], 1.0)
-        pz = core.eval_ic(core.IC_RH54, (w, -w), pfx)
+        pvx, pfx, pfa, pfm = O.mesh(O.MESH_ICOS_TRI, levels[p], 1.0)
+        pz = O.ic_eval(O.IC_RH54, (w, -w), pfx)
         _, pu = lpm_oracle.bve_vertex_solve(pvx, pfx, pz, pfa, pfm, want_psi=False)
         sums.append((p, float(np.abs(pu).sum())))
     gathered = [None] * world
@@ -74,15 +74,15 @@ def _worker(rank, world, port, out_dir):
 def test_two_rank_sharding_matches_single_rank(tmp_path, oracle):
     import torch.multiprocessing as mp
 
-    from lpm_gb300 import core
+    import lpm_oracle as O
     from lpm_gb300.partition import problem_assignment, target_slice
 
     port = _free_port()
     mp.start_processes(_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True,
                        start_method="spawn")
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     w = 2 * math.pi / 12.5
-    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    fz = O.ic_eval(O.IC_RH54, (w, -w), fx)
     _, u = oracle.bve_vertex_solve(vx, fx, fz, fa, fm, want_psi=False)
     sharded = np.load(tmp_path / "sharded.npy")
     assert np.array_equal(sharded, u)
@@ -101,14 +101,14 @@ def _swe_worker(rank, world, port, out_dir):
     import torch.distributed as dist
 
     import lpm_oracle
-    from lpm_gb300 import core
+    import lpm_oracle as O
     from lpm_gb300.partition import target_slice
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     lpm_oracle.set_threads(1)
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     zeta = np.sin(2 * fx[:, 0]) + fx[:, 2]
     sigma = np.cos(3 * fx[:, 1])
     sl = target_slice(vx.shape[0], world, rank)
@@ -132,12 +132,12 @@ def test_two_rank_swe_sharding_matches_single_rank(tmp_path, oracle):
     the final gather, identical bits."""
     import torch.multiprocessing as mp
 
-    from lpm_gb300 import core
+    import lpm_oracle as O
 
     port = _free_port()
     mp.start_processes(_swe_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True,
                        start_method="spawn")
-    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, 2, 1.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 2, 1.0)
     zeta = np.sin(2 * fx[:, 0]) + fx[:, 2]
     sigma = np.cos(3 * fx[:, 1])
     ref = oracle.swe_sphere_sums(vx, fx, zeta, sigma, fa, fm, 0.02)

@@ -94,9 +94,9 @@ def plane_moment_form(tx, ts, y, zeta, sigma, area, mask, sfc, eps, pse_eps):
 
 
 def test_plane_moment_form_matches_oracle(oracle):
-    from lpm_gb300 import core
+    import lpm_oracle as O
 
-    vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 3, 4.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_QUAD_RECT, 3, 4.0)
     zeta = 2 * np.exp(-np.sum((fx - [1.0, 0.0]) ** 2, 1)) - 2 * np.exp(-np.sum((fx + [1.0, 0.0]) ** 2, 1))
     sigma = 0.3 * np.cos(fx[:, 0]) * np.exp(-np.sum(fx ** 2, 1) / 8)
     fs = 1 + 0.1 * np.exp(-np.sum(fx ** 2, 1))

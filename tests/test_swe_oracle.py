@@ -13,9 +13,9 @@ import numpy as np
 
 
 def _mesh(level):
-    from lpm_gb300 import core
+    import lpm_oracle as O
 
-    vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, level, 4.0)
+    vx, fx, fa, fm = O.mesh(O.MESH_QUAD_RECT, level, 4.0)
     return vx, fx, fa, fm
 
 

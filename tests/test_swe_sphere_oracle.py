@@ -44,9 +44,9 @@ def test_oracle_matches_reference_polynomials(oracle, eps, tag):
 
 
 def _icos(level):
-    from lpm_gb300 import core
+    import lpm_oracle as O
 
-    return core.build_mesh(core.MESH_ICOS_TRI, level, 1.0)
+    return O.mesh(O.MESH_ICOS_TRI, level, 1.0)
 
 
 def test_rotational_velocity_matches_ic2d_and_is_tangent(oracle):
