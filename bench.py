@@ -321,6 +321,8 @@ def run_ours(args, rank, world, device):
         # evaluations of the initial state, error vs the FP64 evaluation ----
         learned = run_learned_eval(args, ctx, stream, base, s64, ipe, device) \
             if not args.no_learned else None
+        c5 = run_c5_leg(args, ctx, stream, device, run_learned_eval.weights) \
+            if learned is not None and not args.no_c5 else None
 
         # ---- accuracy 2: one RK4 step, FP32C vs the same algorithm in FP64
         # (chord form, LPM_FP64_CHORD), same flags; also its throughput ----
@@ -367,7 +369,8 @@ def run_ours(args, rank, world, device):
         core.lib().lpm_bve_rk4_destroy(he)
         e2e_value = 4 * ipe * args.steps / (e2e_ms * 1e-3) / 1e9
 
-        cpu = cpu_baseline(host, args) if not args.no_cpu else None
+        cpu = cpu_baseline(host, args, e2e_value, ipe / (ms64_eval * 1e-3) / 1e9) \
+            if not args.no_cpu else None
 
         result = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
@@ -391,8 +394,12 @@ def run_ours(args, rank, world, device):
                          "frac_of_measured_fp32_fma": round(achieved / fma32, 4)},
             "fp64": {"value": round(ipe / (ms64_eval * 1e-3) / 1e9, 4), "unit": UNIT,
                      "ms_per_evaluation": round(ms64_eval, 2),
+                     "frac_of_measured_fp64_fma": round(
+                         ipe / (ms64_eval * 1e-3) * FLOPS_PER_PAIR / 1e12 / fma64, 4),
                      "note": "one velocity evaluation (vertices + leaf faces) of the initial "
-                             "state, every pair term in the reference's FP64 arithmetic"},
+                             "state in the reference's FP64 kernel (LPM_FP64: cross product "
+                             "out of the sum, Newton-Raphson quotients; 1e-12 parity), "
+                             f"{FLOPS_PER_PAIR} credited flops per pair"},
             "fp64_chord": {"value": round(4 * ipe / (ms64c * 1e-3) / 1e9, 4), "unit": UNIT,
                            "ms_per_step": round(ms64c, 2),
                            "note": "one RK4 step of the FP32C algorithm carried out in FP64"},
@@ -401,6 +408,7 @@ def run_ours(args, rank, world, device):
                                                      "velocity_leaf_faces": e_f},
                 "one_rk4_step_vs_fp64_chord": step_err},
             "learned": learned,
+            "c5_level8_far_field": c5,
             "cpu_baseline": cpu,
         }
     return result
@@ -470,6 +478,7 @@ def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
 
     ms_x = timed_steps(False)
     ms = timed_steps(True)
+    run_learned_eval.weights = ff.get_weights()
     return {"value": round(4 * ipe / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
             "ms_per_step": round(ms, 3), "theta": theta, "rho_min": args.ff_rho_min,
             "train_s": round(train_s, 2),
@@ -485,66 +494,240 @@ def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
                     "fields of icosahedral levels 5-8"}
 
 
-def cpu_baseline(host, args):
-    """FP64 oracle (CPU restatement of the reference functors) on a bounded
-    target sample: n_sample vertex targets against all face slots."""
+C5_SETTINGS = (  # (form, theta, rho_min): the configuration's setting first
+    ("learned", 0.5, 0.25), ("learned", 0.4, 0.30), ("learned", 0.35, 0.30),
+    ("expansion_only", 0.4, None), ("expansion_only", 0.35, None), ("expansion_only", 0.3, None))
+
+
+def run_c5_leg(args, ctx, stream, device, weights):
+    """Configuration C5 inside the default run: icosahedral level 8
+    (1,310,720 leaf faces, 655,362 vertices), Rossby-Haurwitz R = 4,
+    eps = 0.01, RK4 dt = 0.005, the octree far field (leaves <= 64, order-4
+    expansion, exact FP32C near field) with the network trained earlier in
+    this run (its inputs are scale-free: trained on levels 5-8).  For each
+    setting of C5_SETTINGS: one evaluation of 16,384 seeded targets against
+    the GPU FP64 direct sum (reference arithmetic) and the mean of --c5-steps
+    timed RK4 steps after one warm-up step.  The FP64 time per evaluation is
+    the sample's scaled to all targets."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+    from lpm_gb300.farfield import FarField
+
+    L = 8
+    vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, L, 1.0)
+    w = OMEGA / 12.5
+    vz = core.eval_ic(core.IC_RH54, (w, -w), vx)
+    fz = core.eval_ic(core.IC_RH54, (w, -w), fx)
+    nv, nleaf = vx.shape[0], int((fm == 0).sum())
+    ipe = (nv + nleaf) * nleaf
+    st0 = DeviceState((vx, fx, fa, fm, vz, fz), device)
+    xall = torch.cat([st0.vx, st0.fx[st0.fm == 0]])
+    rng = np.random.default_rng(20261203)
+    idx = torch.from_numpy(np.sort(rng.choice(xall.shape[0], 16384, replace=False))).to(device)
+    xs = xall[idx].contiguous()
+    ctx.set_precision(core.FP64)
+    u64 = torch.zeros_like(xs)
+    F.ic2d_passive_sums(ctx, u64, None, xs, st0.fx, st0.fz, st0.fa, st0.fm, EPS)  # warm
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    F.ic2d_passive_sums(ctx, u64, None, xs, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
+    b.record(stream)
+    torch.cuda.synchronize(device)
+    fp64_ms = a.elapsed_time(b) * xall.shape[0] / xs.shape[0]
+    fp64 = ipe / (fp64_ms * 1e-3) / 1e9
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    st = st0.clone()
+    st.velocity(ctx, core.FP64_CHORD)  # entry velocities of the RK4 runs
+    rows = []
+    for form, theta, rho in C5_SETTINGS:
+        ff = FarField(theta=theta, leaf_max=64, rho_min=rho if rho else 0.25, ctx=ctx)
+        ff.set_weights(*weights)
+        ff.set_network(form == "learned")
+        uall = torch.zeros_like(xall)
+        ff.velocity(uall, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
+        torch.cuda.synchronize(device)
+        err = rel_errors(uall[idx], u64)
+        run = st.clone()
+        h = make_stepper(ctx, run, core.FP64_CHORD, flags)
+        core.check(core.lib().lpm_bve_rk4_set_farfield(h, ff.handle, 0))
+        advance(h, run)  # warm: builds the tree
+        torch.cuda.synchronize(device)
+        ms = 0.0
+        for k in range(args.c5_steps):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            advance(h, run)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms += a.elapsed_time(b)
+        core.lib().lpm_bve_rk4_destroy(h)
+        ms /= args.c5_steps
+        rows.append({"form": form, "theta": theta, "rho_min": rho,
+                     "value": round(4 * ipe / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 2),
+                     "error_vs_fp64": err, "network_rows": ff.stats().get("network_rows")
+                     if form == "learned" else 0})
+        ff.close()
+    spec = rows[0]
+    ok = [r for r in rows if r["error_vs_fp64"]["linf"] <= 1e-4]
+    best = {f: max((r for r in ok if r["form"] == f), key=lambda r: r["value"], default=None)
+            for f in ("learned", "expansion_only")}
+    return {"workload": "BVE sphere icosahedral level 8 RK4, Rossby-Haurwitz R=4, eps=0.01, "
+                        "dt=0.005, octree far field (leaves <= 64, order-4 expansion)",
+            "value": spec["value"], "unit": UNIT, "theta": spec["theta"],
+            "rho_min": spec["rho_min"], "error_vs_fp64": spec["error_vs_fp64"],
+            "fp64_direct": {"value": round(fp64, 3), "unit": UNIT,
+                            "ms_per_evaluation": round(fp64_ms, 1),
+                            "note": "GPU FP64 direct sum (reference kernel), 16,384 seeded "
+                                    "targets timed and scaled to all targets"},
+            "speedup_vs_fp64_direct": round(spec["value"] / fp64, 1),
+            "settings": rows,
+            "best_at_1e-4": {f: (None if r is None else
+                                 {"theta": r["theta"], "rho_min": r["rho_min"],
+                                  "value": r["value"], "linf": r["error_vs_fp64"]["linf"]})
+                             for f, r in best.items()},
+            "steps_timed_per_setting": args.c5_steps,
+            "interactions_per_step": 4 * ipe}
+
+
+def make_state_oracle(level: int):
+    """The workload's inputs built by the oracle alone: the reference's mesh
+    (tree_init restated from its seed file) and Gaussian vortex.  The
+    reference arm uses these, so it loads no code of the library; they equal
+    make_state's bit for bit (tests/test_mesh_seeds.py)."""
     sys.path.insert(0, str(ROOT / "oracle"))
+    import lpm_oracle as O
+
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, level, 1.0)
+    params = (4 * math.pi, 4.0, 0.0, 0.05 * math.pi, 0.0, OMEGA)
+    vz = O.ic_eval(O.IC_GAUSSIAN_SPHERE, params, vx)
+    fz = O.ic_eval(O.IC_GAUSSIAN_SPHERE, params, fx)
+    return vx, fx, fa, fm, vz, fz
+
+
+CPU_TARGETS_NOTE = ("the reference's Kokkos-OpenMP build cannot be compiled (Kokkos, "
+                    "KokkosKernels, MPI, spdlog, Catch2 absent); this is the FP64 CPU "
+                    "restatement of its functors in oracle/, built -O3 with native code "
+                    "generation for this host (like Kokkos_ARCH_NATIVE), contraction off")
+
+
+def cpu_sample(host, n_sample):
+    vx = host[0]
+    rng = np.random.default_rng(20261203)
+    return np.sort(rng.choice(vx.shape[0], min(n_sample, vx.shape[0]), replace=False))
+
+
+def cpu_time_eval(host, idx, want_psi, reps, warmup):
+    """Seconds per FP64 passive-sum evaluation of the targets idx against all
+    face slots (Incompressible2DPassiveSums, sphere kernel with eps), on every
+    host thread; median of reps runs after warmup runs."""
     import lpm_oracle
 
     vx, fx, fa, fm, vz, fz = host
-    threads = os.cpu_count() or 1
-    lpm_oracle.set_threads(threads)
-    nleaf = int((fm == 0).sum())
-    n_sample = args.cpu_targets
-    idx = np.random.default_rng(20261203).choice(vx.shape[0], n_sample, replace=False)
-    idx.sort()
-    lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx[:256])  # warm
-    t0 = time.perf_counter()
-    lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx)
-    dt = time.perf_counter() - t0
-    pairs = n_sample * nleaf
-    return {"value": round(pairs / dt / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n_sample} seeded vertex targets x {nleaf} leaf sources, one FP64 velocity "
-                      f"evaluation ({dt:.1f} s)"}
+    lpm_oracle.use_native(True)
+    lpm_oracle.set_threads(os.cpu_count() or 1)
+    for _ in range(warmup):
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx, want_psi=want_psi)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx, want_psi=want_psi)
+        ts.append(time.perf_counter() - t0)
+    lpm_oracle.use_native(False)
+    return statistics.median(ts), ts
+
+
+def cpu_baseline(host, args, gpu_fp32c_e2e=None, gpu_fp64=None):
+    """FP64 oracle (CPU restatement of the reference functors) on a bounded
+    target sample: --cpu-targets seeded vertex targets against all face slots,
+    velocity only (the GPU arm's per-pair work), median of 5 after 1 warm-up;
+    the reference kernel's velocity + stream function (one log per pair) once
+    beside it."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    nleaf = int((host[3] == 0).sum())
+    idx = cpu_sample(host, args.cpu_targets)
+    t_u, ts = cpu_time_eval(host, idx, False, 5, 1)
+    t_up, _ = cpu_time_eval(host, idx, True, 1, 0)
+    pairs = idx.size * nleaf
+    value = pairs / t_u / 1e9
+    out = {"value": round(value, 4), "unit": UNIT, "cores": os.cpu_count() or 1,
+           "kind": "port",
+           "sample": f"{idx.size} seeded vertex targets x {nleaf} leaf sources, one FP64 "
+                     f"velocity evaluation (eps kernel, velocity only as timed on the GPU), "
+                     f"median of 5 after 1 warm-up: {t_u:.2f} s "
+                     f"(runs {', '.join(f'{t:.2f}' for t in ts)})",
+           "with_stream_function": {"value": round(pairs / t_up / 1e9, 4), "unit": UNIT,
+                                    "note": "the reference's passive-sum kernel as written "
+                                            "(velocity and stream function, one log per pair)"},
+           "note": CPU_TARGETS_NOTE}
+    if gpu_fp32c_e2e is not None:
+        out["gpu_fp32c_e2e_over_cpu_fp64"] = round(gpu_fp32c_e2e / value, 1)
+    if gpu_fp64 is not None:
+        out["gpu_fp64_over_cpu_fp64"] = round(gpu_fp64 / value, 2)
+    return out
 
 
 # ---------------------------------------------------------------------------
 # reference arm: the reference's CPU algorithm (FP64 port; the Kokkos build is
-# not buildable here), on this workload, all host threads
+# not buildable here), on this workload, all host threads; inputs and code
+# from oracle/ only
 # ---------------------------------------------------------------------------
 def run_reference(args):
     sys.path.insert(0, str(ROOT / "oracle"))
     import lpm_oracle
 
-    host = make_state(args.level)
+    host = make_state_oracle(args.level)
     vx, fx, fa, fm, vz, fz = host
     nv, nleaf = vx.shape[0], int((fm == 0).sum())
     threads = os.cpu_count() or 1
+    idx = cpu_sample(host, args.cpu_targets)
+    lpm_oracle.use_native(True)
     lpm_oracle.set_threads(threads)
-    n_sample = args.cpu_targets
-    rng = np.random.default_rng(20261203)
-    idx = np.sort(rng.choice(vx.shape[0], n_sample, replace=False))
     for _ in range(max(args.warmup, 0)):
-        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx[:512])
-    t0 = time.perf_counter()
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx, want_psi=False)
+    ts = []
     for _ in range(args.steps):
-        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx)
-    dt = time.perf_counter() - t0
-    value = args.steps * n_sample * nleaf / dt / 1e9
-    sample = (f"each step: one FP64 velocity evaluation of {n_sample} seeded vertex targets x "
-              f"{nleaf} leaf sources (a bounded sample of the RK4 step)")
+        t0 = time.perf_counter()
+        lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx, want_psi=False)
+        ts.append(time.perf_counter() - t0)
+    dt = sum(ts)
+    t0 = time.perf_counter()
+    lpm_oracle.ic2d_passive_sums(vx, fx, fz, fa, fm, EPS, tgt_idx=idx, want_psi=True)
+    t_up = time.perf_counter() - t0
+    lpm_oracle.use_native(False)
+    pairs = idx.size * nleaf
+    value = args.steps * pairs / dt / 1e9
+    sample = (f"each step: one FP64 velocity evaluation (eps kernel, velocity only: the "
+              f"GPU arm's per-pair work) of {idx.size} seeded vertex targets x {nleaf} leaf "
+              f"sources, a bounded sample of the RK4 step; median step "
+              f"{statistics.median(ts):.2f} s")
+    loaded = []
+    try:
+        with open("/proc/self/maps") as f:
+            loaded = sorted({ln.split()[-1] for ln in f if ln.rstrip().endswith(".so")
+                             and str(ROOT) in ln})
+    except OSError:
+        pass
     return {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic", "config": workload_config(args.level, nv, nleaf),
+            "data": "synthetic (the reference's icosahedral mesh from its seed file, "
+                    "Gaussian vortex; built by oracle/)",
+            "config": workload_config(args.level, nv, nleaf),
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
-                             "kind": "port", "sample": sample},
+                             "kind": "port", "sample": sample,
+                             "with_stream_function": {
+                                 "value": round(pairs / t_up / 1e9, 4), "unit": UNIT,
+                                 "note": "the reference's passive-sum kernel as written "
+                                         "(velocity and stream function, one log per pair)"}},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "the reference's Kokkos-OpenMP build cannot be compiled (Kokkos, "
-                    "KokkosKernels, MPI, spdlog, Catch2 absent); this is the FP64 CPU "
-                    "restatement of its functors in oracle/"}
+            "libraries_loaded_from_repo": loaded,
+            "note": CPU_TARGETS_NOTE}
 
 
 def run_ensemble(args, device):
@@ -604,6 +787,7 @@ def run_ensemble(args, device):
                                    "levels 3-6, 1-4 Gaussian vortices each, eps=0.01, dt=0.005",
                        "levels_histogram": {int(l): int((levels == l).sum()) for l in range(3, 7)},
                        "interactions_per_step": 4 * ipe, "chunk_len": info["chunk_len"],
+                       "kernel_shape": "%d threads x %d targets" % ens.shape(),
                        "work_items_per_evaluation": info["items"], "autotune_s": round(tune_s, 2)},
             "roofline": {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2),
                          "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
@@ -696,6 +880,76 @@ def c3_roofline(device, pairs_per_s: float) -> dict:
             "flops_per_pair_credited": 16,
             "xu_bound_pairs_per_s": xu_pairs, "frac_of_xu_bound": round(pairs_per_s / xu_pairs, 4),
             "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"}
+
+
+def run_fp64(args, device):
+    """The metric's plain-FP64 leg on its own: one velocity evaluation of
+    every vertex and face slot (Incompressible2DPassiveSums +
+    Incompressible2DActiveSums with the BVE face rule, eps = 0.01) of the C2
+    workload at --level, LPM_FP64 (the reference kernel, cross product taken
+    out of the sum) and, once, LPM_FP64_EXACT (every pair term in the
+    reference's operation order) beside it.  value = interactions/s of
+    LPM_FP64, mean of --steps evaluations after --warmup; roofline: 24
+    credited flops per pair against the measured FP64 FMA peak."""
+    import torch
+
+    from lpm_gb300 import build as B
+    from lpm_gb300 import core
+
+    B.build()
+    torch.cuda.set_device(device)
+    ctx = core.Context(device)
+    stream = torch.cuda.current_stream(device)
+    ctx.set_stream(stream)
+    vx, fx, fa, fm, vz, fz = make_state(args.level)
+    nv, nleaf = vx.shape[0], int((fm == 0).sum())
+    ipe = (nv + nleaf) * nleaf
+    st = DeviceState((vx, fx, fa, fm, vz, fz), device)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+
+    def timed(precision, n, warm):
+        for _ in range(warm):
+            st.velocity(ctx, precision)
+        torch.cuda.synchronize(device)
+        ms = 0.0
+        for k in range(n):
+            flush.fill_(float(k))
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            st.velocity(ctx, precision)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms += a.elapsed_time(b)
+        return ms / max(n, 1)
+
+    sampler = ClockSampler(device)
+    sampler.start()
+    l0 = ctx.kernel_launches
+    ms = timed(core.FP64, args.steps, args.warmup)
+    clocks = sampler.stop()
+    launches = ctx.kernel_launches - l0
+    u64 = (st.vu.clone(), st.fu.clone())
+    ms_exact = timed(core.FP64_EXACT, 1, 0)
+    err = {"velocity_vertices": rel_errors(u64[0], st.vu),
+           "velocity_leaf_faces": rel_errors(u64[1], st.fu, st.fm)}
+    fma64 = ctx.fma_peak_tflops(core.FP64)
+    value = ipe / (ms * 1e-3) / 1e9
+    ach = value * FLOPS_PER_PAIR / 1e3
+    return {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (generated icosahedral mesh + Gaussian vortex; no dataset)",
+            "config": dict(workload_config(args.level, nv, nleaf),
+                           step="one velocity evaluation of every target (FP64)"),
+            "roofline": {"bound": "fp64", "achieved": round(ach, 4), "peak": round(fma64, 4),
+                         "unit": "TFLOP/s", "frac": round(ach / fma64, 4), "traffic": None,
+                         "kernel": "nbody_f64h (reference kernel, cross product hoisted)",
+                         "flops_per_pair_credited": FLOPS_PER_PAIR,
+                         "peak_kind": "measured FP64 FMA microbenchmark (lpm_measure_fma_peak)"},
+            "fp64_exact": {"value": round(ipe / (ms_exact * 1e-3) / 1e9, 3),
+                           "ms_per_evaluation": round(ms_exact, 2),
+                           "difference_from_fp64": err},
+            "clocks": clocks, "gpu_launches": launches}
 
 
 def run_plane(args, device):
@@ -1210,7 +1464,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--level", type=int, default=LEVEL)
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5", "swe"], default="c2",
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5", "swe", "fp64"],
+                    default="c2",
                     help="c2: the metric's workload (default); c1: FP64 level 4; "
                          "c3: planar dipoles; c4: 256-problem ensemble; "
                          "c5: level 8 on the learned octree far field; "
@@ -1230,10 +1485,14 @@ def main():
                     help="c5: load a saved network instead of training")
     ap.add_argument("--plane-level", type=int, default=9)
     ap.add_argument("--problems", type=int, default=256)
-    ap.add_argument("--cpu-targets", type=int, default=8192)
+    ap.add_argument("--cpu-targets", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="c2: skip the learned far-field evaluation")
+    ap.add_argument("--no-c5", action="store_true",
+                    help="c2: skip the level-8 far-field leg (configuration C5)")
+    ap.add_argument("--c5-steps", type=int, default=3,
+                    help="c2: timed RK4 steps per far-field setting of the level-8 leg")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the FP32C steps only (for profiler runs)")
     args = ap.parse_args()
@@ -1263,6 +1522,8 @@ def main():
         res = run_c5(args, local) if rank == 0 else {}
     elif args.config == "swe":
         res = run_swe(args, local) if rank == 0 else {}
+    elif args.config == "fp64":
+        res = run_fp64(args, local) if rank == 0 else {}
     else:
         res = run_ours(args, rank, world, local)
     if rank == 0:

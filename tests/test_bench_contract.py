@@ -24,6 +24,11 @@ def test_reference_arm_json_line():
     assert d["value"] > 0 and d["unit"] == "Ginteractions/s"
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+    # the reference arm runs the oracle on the oracle's own inputs: no library
+    # of the product is loaded
+    libs = d["libraries_loaded_from_repo"]
+    assert libs and all("/oracle/build/" in p for p in libs), libs
+    assert not any("lpm_gb300" in p for p in libs)
 
 
 def test_bench_arguments_parse():
