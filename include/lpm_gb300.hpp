@@ -1,8 +1,8 @@
 // lpm_gb300.hpp -- header-only C++17 facade over the C ABI (lpm_gb300.h) with
 // the reference's class and method names.
 //
-// A reference build swaps its Kokkos launches for these calls (see
-// INTEGRATION.md).  The facade needs no Kokkos: any view type with .data()
+// A reference build swaps its Kokkos functor launches for these calls, one
+// call per launch site.  The facade needs no Kokkos: any view type with .data()
 // and .stride(0)/.stride(1) (Kokkos::View<Real*[3]> in either layout, or the
 // small DeviceArray below) converts to an lpm_view.  Nonzero status codes
 // become std::runtime_error, as LPM_REQUIRE does (src/lpm_assert.hpp:22-30).

@@ -49,6 +49,35 @@ class BVESphere:
         self._omg_set = False
         self.t = 0.0
 
+    # ---- checkpoint / restart ------------------------------------------
+    # The reference has no restart for this path; the state of a run is the
+    # particle arrays below plus Omega and t (the steppers keep nothing
+    # between steps), so a snapshot of them resumes a run bit for bit.
+    _STATE = ("vert_x", "rel_vort_verts", "abs_vort_verts", "stream_fn_verts", "velocity_verts",
+              "face_x", "rel_vort_faces", "abs_vort_faces", "stream_fn_faces", "velocity_faces",
+              "face_area", "face_mask")
+
+    def save(self, path) -> None:
+        """Writes the particle state, Omega and t to an .npz file."""
+        arrays = {k: getattr(self, k).cpu().numpy() for k in self._STATE}
+        np.savez(path, Omega=self.Omega, t=self.t, omega_set=self._omg_set,
+                 host_vert_x=self.host_vert_x, host_face_x=self.host_face_x, **arrays)
+
+    @classmethod
+    def from_snapshot(cls, path, ctx=None, device: int = 0) -> "BVESphere":
+        """A BVESphere holding the state written by save()."""
+        self = cls.__new__(cls)
+        self.ctx = ctx if ctx is not None else default_context(device)
+        self.dev = torch.device("cuda", self.ctx.device)
+        with np.load(path) as z:
+            for k in self._STATE:
+                setattr(self, k, torch.from_numpy(z[k]).to(self.dev))
+            self.host_vert_x, self.host_face_x = z["host_vert_x"], z["host_face_x"]
+            self.host_face_area, self.host_face_mask = z["face_area"], z["face_mask"]
+            self.Omega, self.t = float(z["Omega"]), float(z["t"])
+            self._omg_set = bool(z["omega_set"])
+        return self
+
     def n_vertices_host(self) -> int:
         return int(self.vert_x.shape[0])
 

@@ -110,7 +110,6 @@ int check_view(const lpm_view& v, int64_t n, const char* what, bool nullable) {
 
 int check_ctx(lpm_context* ctx) {
   if (!ctx) return fail(LPM_ERR_ARG, "null context");
-  cudaSetDevice(ctx->device);
   return LPM_OK;
 }
 
@@ -137,6 +136,7 @@ int bve_sum(lpm_context* ctx, double* psi, lpm_view u, lpm_view tx,
             const double* area, const uint8_t* mask, int64_t nf, bool wu,
             bool wp) {
   if (int r = check_ctx(ctx)) return r;
+  lpm::DeviceGuard device_guard(ctx->device);
   if (int r = check_sources(fx, zeta, area, mask, nf)) return r;
   if (bad_count(nt)) return fail(LPM_ERR_ARG, "target count out of range");
   if (int r = check_view(tx, nt, "target coordinates", false)) return r;
@@ -175,7 +175,8 @@ int lpm_context_create(lpm_context** out, int device) {
       return fail(LPM_ERR_CUDA, "lpm_context_create: no CUDA device is visible");
     }
     if (device < 0 || device >= n) return fail(LPM_ERR_ARG, "lpm_context_create: bad device id");
-    LPM_CUDA(cudaSetDevice(device));
+    lpm::DeviceGuard device_guard(device);
+    LPM_CUDA(device_guard.status);
     auto* c = new lpm_context();
     c->device = device;
     cudaDeviceProp prop;
@@ -192,7 +193,7 @@ int lpm_context_create(lpm_context** out, int device) {
 
 int lpm_context_destroy(lpm_context* ctx) {
   if (!ctx) return LPM_OK;
-  cudaSetDevice(ctx->device);
+  lpm::DeviceGuard device_guard(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   ctx->arena.release();
   if (ctx->d_err) cudaFree(ctx->d_err);
@@ -208,9 +209,11 @@ int lpm_context_set_stream(lpm_context* ctx, void* stream) {
 
 int lpm_context_set_precision(lpm_context* ctx, int precision) {
   if (!ctx) return fail(LPM_ERR_ARG, "null context");
-  if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD)
+  if (precision != LPM_FP64 && precision != LPM_FP32C && precision != LPM_FP64_CHORD &&
+      precision != LPM_FP64_EXACT)
     return fail(LPM_ERR_ARG,
-                "precision must be LPM_FP64 (64), LPM_FP64_CHORD (65) or LPM_FP32C (32)");
+                "precision must be LPM_FP64 (64), LPM_FP64_CHORD (65), LPM_FP64_EXACT (66) "
+                "or LPM_FP32C (32)");
   ctx->precision = precision;
   return LPM_OK;
 }
@@ -218,6 +221,7 @@ int lpm_context_set_precision(lpm_context* ctx, int precision) {
 int lpm_context_synchronize(lpm_context* ctx) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::check_device_error(*ctx);
     return LPM_OK;
   } catch (...) {
@@ -306,6 +310,7 @@ int lpm_bve_vorticity_tendency(lpm_context* ctx, double* dzeta, lpm_view u,
                                int64_t n, double dt, double Omega) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (bad_count(n)) return fail(LPM_ERR_ARG, "count out of range");
     if (n > 0 && !dzeta) return fail(LPM_ERR_ARG, "null output");
     if (int r = check_view(u, n, "velocity", false)) return r;
@@ -322,6 +327,7 @@ int lpm_ic2d_passive_sums(lpm_context* ctx, int ndim, lpm_view u, double* psi,
                           const uint8_t* mask, double eps, int64_t n_active) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (ndim != LPM_SPHERE && ndim != LPM_PLANE) return fail(LPM_ERR_ARG, "ndim must be 2 or 3");
     if (!std::isfinite(eps) || eps < 0) return fail(LPM_ERR_ARG, "eps must be finite and >= 0");
     if (int r = check_sources(y, zeta, area, mask, n_active)) return r;
@@ -346,6 +352,7 @@ int lpm_ic2d_active_sums(lpm_context* ctx, int ndim, lpm_view u, double* psi,
                          int self_rule) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (ndim != LPM_SPHERE && ndim != LPM_PLANE) return fail(LPM_ERR_ARG, "ndim must be 2 or 3");
     if (!std::isfinite(eps) || eps < 0) return fail(LPM_ERR_ARG, "eps must be finite and >= 0");
     if (self_rule != 0 && self_rule != 1) return fail(LPM_ERR_ARG, "self_rule must be 0 or 1");
@@ -369,6 +376,7 @@ int lpm_ic2d_tendencies(lpm_context* ctx, int ndim, double* dzeta, lpm_view u,
                         int64_t n, double cor) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (ndim != LPM_SPHERE && ndim != LPM_PLANE) return fail(LPM_ERR_ARG, "ndim must be 2 or 3");
     if (bad_count(n)) return fail(LPM_ERR_ARG, "count out of range");
     if (n > 0 && !dzeta) return fail(LPM_ERR_ARG, "null output");
@@ -384,6 +392,7 @@ int lpm_sphere_tangency(lpm_context* ctx, double* udotx, lpm_view x, lpm_view u,
                         int64_t n) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (bad_count(n)) return fail(LPM_ERR_ARG, "count out of range");
     if (n > 0 && !udotx) return fail(LPM_ERR_ARG, "null output");
     if (int r = check_view(x, n, "positions", false)) return r;
@@ -400,6 +409,7 @@ int lpm_ic2d_invariants(lpm_context* ctx, int ndim, int64_t nfaces,
                         const uint8_t* mask, double out[3]) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (ndim != LPM_SPHERE && ndim != LPM_PLANE) return fail(LPM_ERR_ARG, "ndim must be 2 or 3");
     if (!out) return fail(LPM_ERR_ARG, "null output");
     if (bad_count(nfaces)) return fail(LPM_ERR_ARG, "count out of range");
@@ -417,6 +427,7 @@ int lpm_err_norms(lpm_context* ctx, int ndim, int64_t n, lpm_view appx,
                   double out[3]) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (ndim < 1 || ndim > 3) return fail(LPM_ERR_ARG, "ndim must be 1, 2 or 3");
     if (!out) return fail(LPM_ERR_ARG, "null output");
     if (bad_count(n)) return fail(LPM_ERR_ARG, "count out of range");
@@ -464,9 +475,23 @@ int lpm_ic_eval(int kind, const double* params, int nparams, int ndim,
   }
 }
 
+int lpm_wait_selftest(lpm_context* ctx, int spin_limit) {
+  try {
+    if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
+    if (spin_limit < 1 || spin_limit > (1 << 20))
+      return fail(LPM_ERR_ARG, "lpm_wait_selftest: spin_limit must be in [1, 2^20]");
+    lpm::wait_selftest(*ctx, unsigned(spin_limit));
+    return LPM_OK;
+  } catch (...) {
+    return lpm::handle_exception();
+  }
+}
+
 int lpm_measure_fma_peak(lpm_context* ctx, int precision, double* tflops) {
   try {
     if (int r = check_ctx(ctx)) return r;
+    lpm::DeviceGuard device_guard(ctx->device);
     if (!tflops) return fail(LPM_ERR_ARG, "null output");
     if (precision != LPM_FP64 && precision != LPM_FP32C)
       return fail(LPM_ERR_ARG, "bad precision");

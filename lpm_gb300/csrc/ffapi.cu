@@ -67,7 +67,7 @@ int lpm_farfield_create(lpm_context* ctx, lpm_farfield** out, double theta, int 
   if (!(rho_min >= 0 && rho_min <= theta))
     return fail(LPM_ERR_ARG, "lpm_farfield_create: rho_min must be in [0, theta]");
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm_farfield* f = new lpm_farfield();
     f->ctx = ctx;
     f->theta = theta;
@@ -83,7 +83,7 @@ int lpm_farfield_create(lpm_context* ctx, lpm_farfield** out, double theta, int 
 int lpm_farfield_destroy(lpm_farfield* ff) {
   if (!ff) return LPM_OK;
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     cudaStreamSynchronize(ff->ctx->stream);
     delete ff->net;
     ff->net = nullptr;
@@ -111,7 +111,7 @@ int lpm_farfield_train(lpm_farfield* ff, int64_t nsamples, int epochs, int batch
   if (nsamples < 128 || nsamples > (int64_t(1) << 31) - 1)
     return fail(LPM_ERR_ARG, "lpm_farfield_train: nsamples out of range");
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     lpm::TrainCfg c{nsamples, epochs, batch, lr, seed, level_min, level_max, eps};
     const std::vector<float> h = ff->train(c);
     if (loss)
@@ -134,7 +134,7 @@ int lpm_farfield_get_weights(lpm_farfield* ff, float* w, float* norm) {
 int lpm_farfield_set_weights(lpm_farfield* ff, const float* w, const float* norm) {
   if (!ff || !w || !norm) return fail(LPM_ERR_ARG, "null argument");
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     ff->w.assign(w, w + lpm::kNParam);
     ff->norm.assign(norm, norm + LPM_FF_NNORM);
     ff->upload_net();
@@ -148,7 +148,7 @@ int lpm_farfield_set_weights(lpm_farfield* ff, const float* w, const float* norm
 int lpm_farfield_grad(lpm_farfield* ff, const float* x, const float* y, int n, float* grad) {
   if (!ff || !x || !y || !grad) return fail(LPM_ERR_ARG, "null argument");
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     ff->grad(x, y, n, grad);
     return LPM_OK;
   } catch (...) {
@@ -167,7 +167,7 @@ int lpm_farfield_velocity(lpm_farfield* ff, lpm_view u, lpm_view x, int64_t nx, 
   if (!(eps >= 0) || !std::isfinite(eps)) return fail(LPM_ERR_ARG, "eps must be finite and >= 0");
   try {
     lpm_context& c = *ff->ctx;
-    cudaSetDevice(c.device);
+    lpm::DeviceGuard device_guard(c.device);
     c.arena.reset();
     c.arena.reserve(sizeof(int) * (2 * size_t(nf) + 2 * size_t(nf) / 1024 + 8) +
                     sizeof(double4_16a) * size_t(nf + nx) + sizeof(double) * 3 * size_t(nx) + 8192);
@@ -211,7 +211,7 @@ int lpm_farfield_stats(lpm_farfield* ff, int64_t* out) {
   if (!ff || !out) return fail(LPM_ERR_ARG, "null argument");
   if (!ff->built()) return fail(LPM_ERR_STATE, "far field: no evaluation yet");
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     ff->counts();
     out[0] = ff->last_far;
     out[1] = ff->last_near;
@@ -230,7 +230,7 @@ int lpm_farfield_timing(lpm_farfield* ff, int enable, double* tree_ms, double* n
                         int64_t* evals) {
   if (!ff) return fail(LPM_ERR_ARG, "null far field");
   try {
-    cudaSetDevice(ff->ctx->device);
+    lpm::DeviceGuard device_guard(ff->ctx->device);
     double a = 0, b = 0;
     int64_t n = 0;
     ff->timings(&a, &b, &n);
@@ -309,7 +309,7 @@ int lpm_mesh_build_device(lpm_context* ctx, int kind, int level, double radius, 
   if (level < 0 || level > 10) return fail(LPM_ERR_ARG, "mesh level out of range [0, 10]");
   if (!(radius > 0) || !std::isfinite(radius)) return fail(LPM_ERR_ARG, "radius must be positive");
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::mesh_build_device(*ctx, kind, level, radius, vx, fx, farea, fmask);
     return LPM_OK;
   } catch (...) {
@@ -321,7 +321,7 @@ int lpm_tc_selftest(lpm_context* ctx, const float* A, const float* B, float* D, 
                     int a_mn, int b_mn) {
   if (!ctx || !A || !B || !D) return fail(LPM_ERR_ARG, "null argument");
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::tc_selftest(*ctx, A, B, D, N, K, a_mn, b_mn);
     lpm::check_device_error(*ctx);
     return LPM_OK;

@@ -51,6 +51,27 @@ namespace lpm {
                                            cudaGetErrorString(e_));       \
   } while (0)
 
+// Makes `device` current for the lifetime of the guard and then restores the
+// device that was current before, so an entry point never leaves the calling
+// thread on a different GPU.  status holds cudaSetDevice's result.
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t status = cudaSuccess;
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != device) {
+      status = cudaSetDevice(device);
+    } else {
+      prev = -1;  // already current: nothing to restore
+    }
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 // Strided FP64 view, same layout as lpm_view.
 struct View {
   double* p;
@@ -196,6 +217,10 @@ void invariants(lpm_context& ctx, int ndim, int64_t n, const double* zeta,
 void err_norms(lpm_context& ctx, int ndim, int64_t n, View appx, View exact,
                const double* wt, const uint8_t* mask, double out[3]);
 double fma_peak(lpm_context& ctx, int precision);
+// One CTA whose tile wait cannot complete: it arms the tile pipeline's
+// mbarrier for a copy that is never issued, gives up after `spin` polls, sets
+// the context's device error flag, drains (bounded) and returns.
+void wait_selftest(lpm_context& ctx, unsigned spin);
 // Uniform mesh built on the device (mesh_dev.cu); device output arrays.
 void mesh_build_device(lpm_context& ctx, int kind, int level, double radius, double* vx,
                        double* fx, double* farea, uint8_t* fmask);

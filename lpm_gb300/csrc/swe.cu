@@ -826,7 +826,7 @@ int lpm_swe_plane_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot, double
                        fx, fzeta, fsigma, farea, fmask, fs, nf, eps, pse_eps, do_velocity))
     return r;
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::SweOut o{lpm::to_view(u), ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, do_velocity};
     lpm::swe_plane_sums(*ctx, lpm::to_view(vx), vs, nv, lpm::to_view(fx), fzeta, fsigma, farea,
                         fmask, fs, nf, eps, pse_eps, false, o);
@@ -846,7 +846,7 @@ int lpm_swe_plane_face_sums(lpm_context* ctx, lpm_view u, double* ddot, double* 
                        fx, fzeta, fsigma, farea, fmask, fs, nf, eps, pse_eps, do_velocity))
     return r;
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::SweOut o{lpm::to_view(u), ddot, du1dx1, du1dx2, du2dx1, du2dx2, laps, psi, phi, do_velocity};
     // PlanarSWEFaceSums: collocated = FloatingPoint<Real>::zero(eps)
     lpm::swe_plane_sums(*ctx, lpm::to_view(fx), fs, nf, lpm::to_view(fx), fzeta, fsigma, farea,
@@ -870,7 +870,7 @@ int lpm_swe_sphere_vertex_sums(lpm_context* ctx, lpm_view u, double* ddot, doubl
     return lpm::fail(LPM_ERR_ARG, "null source array");
   if (!(eps >= 0) || !std::isfinite(eps)) return lpm::fail(LPM_ERR_ARG, "eps must be finite and >= 0");
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     lpm::swe_sphere_sums(*ctx, lpm::to_view(vx), nv, lpm::to_view(fx), fzeta, fsigma, farea, fmask,
                          nf, eps, false, lpm::to_view(u), ddot, grad, do_velocity);
     return LPM_OK;
@@ -889,7 +889,7 @@ int lpm_swe_sphere_face_sums(lpm_context* ctx, lpm_view u, double* ddot, double*
     return lpm::fail(LPM_ERR_ARG, "null input or output array");
   if (!(eps >= 0) || !std::isfinite(eps)) return lpm::fail(LPM_ERR_ARG, "eps must be finite and >= 0");
   try {
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     // SphereFaceSums: collocated = FloatingPoint<Real>::zero(eps)
     lpm::swe_sphere_sums(*ctx, lpm::to_view(fx), nf, lpm::to_view(fx), fzeta, fsigma, farea, fmask,
                          nf, eps, lpm::fp_zero(eps), lpm::to_view(u), ddot, grad, do_velocity);
