@@ -10,8 +10,13 @@
 // spad[p]) of the packed sources (its unmasked faces, zero-padded to a whole
 // number of tiles) and its own block of chunk partials.  The work list is
 // sorted by decreasing chunk length, so the persistent CTAs drain it
-// longest-first and the tail stays short.  The chunk length is chosen by an
-// autotuner that times one evaluation per candidate at set-up.
+// longest-first and the tail stays short.  The chunk length and the FP32
+// kernel shape (threads x targets per thread, the kF32Shapes of the
+// single-problem kernel) are chosen by an autotuner that times one
+// evaluation per candidate at set-up: chunk lengths with the default shape,
+// then the shapes at the best length.  A target's sums do not depend on the
+// shape (each target is summed by one thread in source order), so only the
+// chunk length changes results in the last bits.
 //
 // Only the chord-form velocity is evaluated (LPM_FP32C or LPM_FP64_CHORD);
 // the reference-arithmetic FP64 path runs one problem at a time through
@@ -31,8 +36,8 @@ namespace lpm {
 namespace {
 
 // Persistent chord-form velocity kernel over the work list.
-template <typename T, int R, int NT, int TILE>
-__global__ void __launch_bounds__(NT)
+template <typename T, int R, int NT, int TILE, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     ens_nbody(const int4* __restrict__ items, int nitems, int* counter,
               const typename Vec4<T>::type* __restrict__ tgt,
               const typename SrcRec<T>::type* __restrict__ src, const int64_t* ptoff,
@@ -137,7 +142,8 @@ struct lpm_ensemble {
   void *tgt = nullptr, *src = nullptr;
   double* part = nullptr;
   double* buf = nullptr;  // xs[4] (3T each), zs[4] (T each), xw (3T)
-  int occ = 1;
+  int shape = 0;         // FP32 kernel shape (index into kF32Shapes)
+  int occ_shape[lpm::kNumF32Shapes] = {};  // resident CTAs per SM, per shape
   // graph
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -146,7 +152,13 @@ struct lpm_ensemble {
   std::vector<cudaEvent_t> timers;
 
   bool f32() const { return precision == LPM_FP32C; }
-  int tb() const { return f32() ? lpm::F32_NT * lpm::F32_R : lpm::F64_NT * lpm::F64_R; }
+  // target padding unit (every FP32 shape divides F32_TB)
+  int tb() const { return f32() ? lpm::F32_TB : lpm::F64_NT * lpm::F64_R; }
+  // targets per CTA of the kernel in use
+  int cta_targets() const {
+    return f32() ? lpm::kF32Shapes[shape].nt * lpm::kF32Shapes[shape].r
+                 : lpm::F64_NT * lpm::F64_R;
+  }
   int tile() const { return f32() ? lpm::F32_TILE : lpm::F64_TILE; }
 
   void* dalloc(size_t bytes) {
@@ -222,20 +234,35 @@ struct lpm_ensemble {
     LPM_CUDA(cudaMemset(src, 0, 32 * S));
     counter = static_cast<int*>(dalloc(sizeof(int)));
     buf = static_cast<double*>(dalloc(sizeof(double) * size_t(T) * 19));
-    if (f32())
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &occ, lpm::ens_nbody<float, lpm::F32_R, lpm::F32_NT, lpm::F32_TILE>, lpm::F32_NT, 0);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &occ, lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE>, lpm::F64_NT, 0);
-    occ = std::max(occ, 1);
+    if (f32()) {
+      static_assert(lpm::kF32Shapes[0].nt == 256 && lpm::kF32Shapes[0].r == 4 &&
+                        lpm::kF32Shapes[1].nt == 256 && lpm::kF32Shapes[1].r == 4 &&
+                        lpm::kF32Shapes[2].nt == 128 && lpm::kF32Shapes[2].r == 8 &&
+                        lpm::kF32Shapes[3].nt == 256 && lpm::kF32Shapes[3].r == 2,
+                    "ensemble launch table out of sync with kF32Shapes");
+      occupancy(0, lpm::ens_nbody<float, 4, 256, lpm::F32_TILE, 3>, 256);
+      occupancy(1, lpm::ens_nbody<float, 4, 256, lpm::F32_TILE, 4>, 256);
+      occupancy(2, lpm::ens_nbody<float, 8, 128, lpm::F32_TILE, 4>, 128);
+      occupancy(3, lpm::ens_nbody<float, 2, 256, lpm::F32_TILE, 5>, 256);
+    } else {
+      occupancy(0, lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE, 1>,
+                lpm::F64_NT);
+    }
     LPM_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
   }
 
-  // Work list and partial layout for a chunk length (in sources).
+  template <class K>
+  void occupancy(int k, K kernel, int nt) {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, nt, 0);
+    occ_shape[k] = std::max(v, 1);
+  }
+
+  // Work list and partial layout for a chunk length (in sources) and the
+  // current kernel shape: one item per (problem, CTA target block, chunk).
   void plan(int chunk) {
     chunk_len = chunk;
-    const int TB = tb();
+    const int TB = cta_targets();
     std::vector<int64_t> ppart(nprob);
     std::vector<int> pch(nprob);
     struct It {
@@ -311,7 +338,7 @@ struct lpm_ensemble {
   void nbody() {
     lpm_context& c = *ctx;
     LPM_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), c.stream));
-    const int grid = c.num_sms * occ;
+    const int grid = c.num_sms * occ_shape[f32() ? shape : 0];
     cudaEvent_t e[2];
     const bool timed = flags & LPM_STEP_TIME_NBODY;
     if (timed) {
@@ -319,18 +346,27 @@ struct lpm_ensemble {
       LPM_CUDA(cudaEventCreate(&e[1]));
       LPM_CUDA(cudaEventRecord(e[0], c.stream));
     }
-    if (f32())
-      lpm::ens_nbody<float, lpm::F32_R, lpm::F32_NT, lpm::F32_TILE>
-          <<<grid, lpm::F32_NT, 0, c.stream>>>(
-              items, int(nitems), counter, static_cast<const float4*>(tgt),
-              static_cast<const lpm::SrcF32*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
-              chunk_len, float(c0()), part, c.d_err);
-    else
-      lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE>
+    if (f32()) {
+      switch (shape) {
+        case 1:
+          launch_f32<4, 256, 4>(grid);
+          break;
+        case 2:
+          launch_f32<8, 128, 4>(grid);
+          break;
+        case 3:
+          launch_f32<2, 256, 5>(grid);
+          break;
+        default:
+          launch_f32<4, 256, 3>(grid);
+      }
+    } else {
+      lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE, 1>
           <<<grid, lpm::F64_NT, 0, c.stream>>>(
               items, int(nitems), counter, static_cast<const double4_16a*>(tgt),
               static_cast<const double4_16a*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
               chunk_len, c0(), part, c.d_err);
+    }
     c.launches++;
     if (timed) {
       LPM_CUDA(cudaEventRecord(e[1], c.stream));
@@ -338,6 +374,14 @@ struct lpm_ensemble {
       timers.push_back(e[1]);
     }
     LPM_CUDA(cudaGetLastError());
+  }
+
+  template <int R, int NT, int MINB>
+  void launch_f32(int grid) {
+    lpm::ens_nbody<float, R, NT, lpm::F32_TILE, MINB><<<grid, NT, 0, ctx->stream>>>(
+        items, int(nitems), counter, static_cast<const float4*>(tgt),
+        static_cast<const lpm::SrcF32*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
+        chunk_len, float(c0()), part, ctx->d_err);
   }
 
   // One evaluation of the current state's velocities into vvel / fvel.
@@ -454,8 +498,7 @@ struct lpm_ensemble {
     LPM_CUDA(cudaEventCreate(&e1));
     const uint32_t saved = flags;
     flags &= ~LPM_STEP_TIME_NBODY;
-    for (int len : cands) {
-      plan(len);
+    auto time_plan = [&]() {
       nbody();  // warm
       LPM_CUDA(cudaEventRecord(e0, ctx->stream));
       nbody();
@@ -463,14 +506,35 @@ struct lpm_ensemble {
       LPM_CUDA(cudaEventSynchronize(e1));
       float ms = 0;
       LPM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms;
+    };
+    // chunk length with the default shape
+    shape = 0;
+    for (int len : cands) {
+      plan(len);
+      const float ms = time_plan();
       if (ms < best) {
         best = ms;
         best_len = len;
       }
     }
+    // kernel shape at that chunk length
+    int best_shape = 0;
+    if (f32()) {
+      for (int k = 1; k < lpm::kNumF32Shapes; ++k) {
+        shape = k;
+        plan(best_len);
+        const float ms = time_plan();
+        if (ms < best) {
+          best = ms;
+          best_shape = k;
+        }
+      }
+    }
     flags = saved;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    shape = best_shape;
     plan(best_len);
     tuned_ms = best;
   }
@@ -517,7 +581,7 @@ int lpm_ensemble_create(lpm_context* ctx, lpm_ensemble** out, int nproblems,
       delete e;
       return lpm::fail(LPM_ERR_ARG, "lpm_ensemble_create: null mask");
     }
-    cudaSetDevice(ctx->device);
+    lpm::DeviceGuard device_guard(ctx->device);
     std::vector<uint8_t> hmask(e->NF);
     LPM_CUDA(cudaMemcpy(hmask.data(), fmask, e->NF, cudaMemcpyDeviceToHost));
     try {
@@ -536,6 +600,7 @@ int lpm_ensemble_create(lpm_context* ctx, lpm_ensemble** out, int nproblems,
 
 int lpm_ensemble_destroy(lpm_ensemble* e) {
   if (!e) return LPM_OK;
+  lpm::DeviceGuard device_guard(e->ctx->device);
   e->free_all();
   delete e;
   return LPM_OK;
@@ -546,7 +611,7 @@ int lpm_ensemble_velocity(lpm_ensemble* e, lpm_view vx, lpm_view vvel, lpm_view 
   try {
     if (!e || !vx.p || !vvel.p || !fx.p || !fzeta || !fvel.p || !farea)
       return lpm::fail(LPM_ERR_ARG, "lpm_ensemble_velocity: null argument");
-    cudaSetDevice(e->ctx->device);
+    lpm::DeviceGuard device_guard(e->ctx->device);
     lpm::EnsTg g = e->targets(vx, nullptr, vvel, fx, const_cast<double*>(fzeta), fvel, farea);
     // vertex vorticity is not read by an evaluation
     if (e->chunk_len == 0) e->autotune(g);
@@ -563,7 +628,7 @@ int lpm_ensemble_advance_timestep(lpm_ensemble* e, lpm_view vx, double* vzeta,
   try {
     if (!e || !vx.p || !vzeta || !vvel.p || !fx.p || !fzeta || !fvel.p || !farea)
       return lpm::fail(LPM_ERR_ARG, "lpm_ensemble_advance_timestep: null argument");
-    cudaSetDevice(e->ctx->device);
+    lpm::DeviceGuard device_guard(e->ctx->device);
     lpm::EnsTg g = e->targets(vx, vzeta, vvel, fx, fzeta, fvel, farea);
     if (e->chunk_len == 0) e->autotune(g);
     e->advance(g);
@@ -582,13 +647,25 @@ int lpm_ensemble_info(lpm_ensemble* e, int64_t* chunk_len, int64_t* items,
   return LPM_OK;
 }
 
+int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread) {
+  if (!e || !threads || !targets_per_thread) return lpm::fail(LPM_ERR_ARG, "null argument");
+  if (e->f32()) {
+    *threads = lpm::kF32Shapes[e->shape].nt;
+    *targets_per_thread = lpm::kF32Shapes[e->shape].r;
+  } else {
+    *threads = lpm::F64_NT;
+    *targets_per_thread = lpm::F64_R;
+  }
+  return LPM_OK;
+}
+
 int lpm_ensemble_set_chunk_len(lpm_ensemble* e, int64_t chunk_len) {
   try {
     if (!e || chunk_len <= 0 || chunk_len > (int64_t(1) << 30))
       return lpm::fail(LPM_ERR_ARG, "lpm_ensemble_set_chunk_len: bad argument");
     if (e->chunk_len != 0)
       return lpm::fail(LPM_ERR_STATE, "lpm_ensemble_set_chunk_len: plan already chosen");
-    cudaSetDevice(e->ctx->device);
+    lpm::DeviceGuard device_guard(e->ctx->device);
     const int64_t tl = e->tile();
     e->plan(int((chunk_len + tl - 1) / tl * tl));
     return LPM_OK;

@@ -18,6 +18,7 @@
 #include <cstdint>
 #include <numeric>
 #include <stdexcept>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -71,6 +72,23 @@ uint64_t key_of(const Box& bx, const double* p) {
   return k;
 }
 
+// Runs jobs(0..count-1) on their own threads; a job whose thread cannot be
+// created (std::system_error, e.g. under a container's thread limit) runs on
+// the calling thread instead.  Returns after every job has finished.
+template <class Job>
+void run_jobs(int count, const Job& job) {
+  std::vector<std::thread> th;
+  th.reserve(count);
+  for (int i = 0; i < count; ++i) {
+    try {
+      th.emplace_back(job, i);
+    } catch (const std::system_error&) {
+      job(i);
+    }
+  }
+  for (auto& t : th) t.join();
+}
+
 // Sorts (key, index) pairs on up to 16 host threads: equal chunks sorted
 // concurrently, then merged pairwise.  The pairs are totally ordered (ties
 // in key broken by index), so the result is the single-threaded one.
@@ -85,18 +103,14 @@ void parallel_sort(std::vector<std::pair<uint64_t, int>>& v) {
   while (p * 2 <= hw) p *= 2;
   std::vector<int64_t> cut(p + 1);
   for (int i = 0; i <= p; ++i) cut[i] = n * i / p;
-  std::vector<std::thread> th;
-  for (int i = 0; i < p; ++i)
-    th.emplace_back([&v, &cut, i] { std::sort(v.begin() + cut[i], v.begin() + cut[i + 1]); });
-  for (auto& t : th) t.join();
+  run_jobs(p, [&v, &cut](int i) { std::sort(v.begin() + cut[i], v.begin() + cut[i + 1]); });
   for (int w = 1; w < p; w *= 2) {
-    th.clear();
-    for (int i = 0; i + w < p; i += 2 * w)
-      th.emplace_back([&v, &cut, i, w, p] {
-        std::inplace_merge(v.begin() + cut[i], v.begin() + cut[i + w],
-                           v.begin() + cut[std::min(i + 2 * w, p)]);
-      });
-    for (auto& t : th) t.join();
+    const int merges = (p - w + 2 * w - 1) / (2 * w);  // i = 0, 2w, ... with i + w < p
+    run_jobs(merges, [&v, &cut, w, p](int m) {
+      const int i = 2 * w * m;
+      std::inplace_merge(v.begin() + cut[i], v.begin() + cut[i + w],
+                         v.begin() + cut[std::min(i + 2 * w, p)]);
+    });
   }
 }
 

@@ -82,6 +82,12 @@ class BVEEnsemble:
         check(lib().lpm_ensemble_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return {"chunk_len": a.value, "items": b.value, "targets": c.value}
 
+    def shape(self):
+        """(threads per CTA, targets per thread) of the N-body kernel in use."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().lpm_ensemble_shape(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def set_chunk_len(self, n: int):
         check(lib().lpm_ensemble_set_chunk_len(self._h, int(n)))
 
