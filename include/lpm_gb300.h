@@ -456,6 +456,20 @@ int lpm_vtk_write_polymesh(const char* path, int ndim, int64_t nv,
                            const double* farea, int nfields,
                            const lpm_vtk_field* fields);
 
+/* NcWriter (src/netcdf/lpm_netcdf_writer.cpp:5-47) with the mesh and field
+ * content of the reference's NetCDF definitions (src/netcdf/lpm_netcdf_impl.hpp),
+ * without the netCDF library: writes a classic-format NetCDF file (64-bit
+ * offsets, CDF-2) with the global attribute LPM, an unlimited "time"
+ * dimension holding one record (time, vertices.phys_crds, faces.phys_crds and
+ * the fields, named by the caller: location 0 = vertices, 1 = face slots;
+ * 1 or ndim components), and the fixed arrays faces.vertices (int),
+ * faces.mask (byte) and faces.area.  All pointers are host memory. */
+int lpm_netcdf_write_polymesh(const char* path, int ndim, int64_t nv,
+                              const double* vx, int64_t nf, int nfv,
+                              const int32_t* fverts, const uint8_t* fmask,
+                              const double* farea, const double* fx, double time,
+                              int nfields, const lpm_vtk_field* fields);
+
 /* ---- octree far field with a learned correction ------------------------- */
 /* No reference counterpart: the reference's octree sources (LpmOctree*,
  * LpmNodeArray*) are not built and src/tree/lpm_cpu_tree's generators are

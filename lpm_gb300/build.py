@@ -22,7 +22,7 @@ LIB = OUT / "liblpm_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["direct_sum.cu", "stepper.cu", "capi.cu", "noalloc.cu", "oneshot.cu", "ensemble.cu", "farfield.cu",
               "mlp.cu", "ffapi.cu", "mesh_dev.cu", "swe.cu"]
-CXX_SOURCES = ["mesh.cpp", "ics.cpp", "tree.cpp", "vtk.cpp"]
+CXX_SOURCES = ["mesh.cpp", "ics.cpp", "tree.cpp", "vtk.cpp", "netcdf.cpp"]
 
 
 def nvcc() -> str:

@@ -68,6 +68,7 @@ EXPORTS = [
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
     "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape",
+    "lpm_netcdf_write_polymesh",
 ]
 
 
@@ -183,6 +184,8 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ensemble_run": [vp, i32, V, vp, V, V, vp, V, vp],
         "lpm_one_call_release": [],
         "lpm_vtk_write_polymesh": [C.c_char_p, i32, i64, vp, vp, i64, i32, vp, vp, vp, i32, vp],
+        "lpm_netcdf_write_polymesh": [C.c_char_p, i32, i64, vp, i64, i32, vp, vp, vp, vp, dbl,
+                                      i32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -89,3 +89,34 @@ class VtkPolymeshInterface:
             None if h is None else h.ctypes.data, self.fverts.shape[0], self.fverts.shape[1],
             self.fverts.ctypes.data, self.fmask.ctypes.data, self.farea.ctypes.data,
             len(self._fields), C.addressof(fields)))
+
+
+class NcPolymeshWriter(VtkPolymeshInterface):
+    """NetCDF output of the same content (NcWriter with the reference's mesh
+    and field names, src/netcdf/lpm_netcdf_writer.cpp,
+    src/netcdf/lpm_netcdf_impl.hpp), written by the library
+    (lpm_netcdf_write_polymesh) in the classic format with 64-bit offsets:
+    one time record of vertices.phys_crds, faces.phys_crds and the added
+    fields (1 or ndim components), and faces.vertices / faces.mask /
+    faces.area.  Cell arrays are given per face slot (all slots written).
+
+        nc = NcPolymeshWriter(vx, fverts, fmask, farea, fx)
+        nc.add_scalar_cell_data(vort_faces, "rel_vort")
+        nc.write("bve_0000.nc", t=0.0)
+    """
+
+    def __init__(self, vx, fverts, fmask, farea, fx):
+        super().__init__(vx, fverts, fmask, farea)
+        self.fx = _host(fx)
+
+    def write(self, path: str, t: float = 0.0) -> None:
+        fields = (_Field * max(1, len(self._fields)))()
+        names = []
+        for k, (name, loc, a) in enumerate(self._fields):
+            names.append(name.encode())
+            fields[k] = _Field(names[-1], loc, a.shape[1], a.ctypes.data)
+        check(lib().lpm_netcdf_write_polymesh(
+            str(path).encode(), self.ndim, self.vx.shape[0], self.vx.ctypes.data,
+            self.fverts.shape[0], self.fverts.shape[1], self.fverts.ctypes.data,
+            self.fmask.ctypes.data, self.farea.ctypes.data, self.fx.ctypes.data, float(t),
+            len(self._fields), C.addressof(fields)))
