@@ -357,9 +357,10 @@ __global__ void k_rk2_mid(TG g, PK k, Rk2Buf b, Rk2Par P) {
   const int64_t T = g.T;
   double pw[3] = {0, 0, 0}, u[3] = {0, 0, 0}, ps = 0;
   for (int c = 0; c < nd; ++c) pw[c] = b.xw[c * T + t];
-  combine(g, k, t, pw, true, P.c0, P.sg, u, &ps);
+  // velocity only: the stage's stream function would be overwritten by the
+  // final evaluation
+  combine(g, k, t, pw, false, P.c0, P.sg, u, &ps);
   for (int c = 0; c < nd; ++c) g.u(t, c) = u[c];
-  if (double* pp = g.psi(t)) *pp = ps;
   const double z2 = ic2d_tend(nd, u, P.cor);
   const double h = dm(0.5, P.dt);
   const double z = da(da(dm(h, b.z1[t]), dm(h, z2)), g.zeta(t));

@@ -174,7 +174,15 @@ struct lpm_stepper_base {
     LPM_CUDA(cudaStreamSynchronize(c.stream));
     ff->build(h.data() + 3 * T, nsrc, h.data(), T);
   }
-  void nbody() {
+  // One N-body evaluation; with_psi = false evaluates the velocity only (a
+  // plan without the stream-function component) even if the stepper wants psi.
+  void nbody(bool with_psi = true) {
+    const bool wp = want_psi && with_psi;
+    lpm::NbodyPlan pl = plan;
+    if (plan.wp && !wp) {
+      pl.wp = false;
+      pl.ncomp = plan.ncomp - 1;
+    }
     if (ff) {
       cudaEvent_t e[2];
       const bool timed = flags & LPM_STEP_TIME_NBODY;
@@ -191,20 +199,20 @@ struct lpm_stepper_base {
       }
       return;
     }
-    if (lpm::mode_of(precision) != lpm::M_REF64 && want_psi && ndim == 3)
+    if (lpm::mode_of(precision) != lpm::M_REF64 && wp && ndim == 3)
       lpm::sum_strengths(*ctx, src, precision == LPM_FP32C, nsrc, sgbuf, sgbuf + 8);
     if (flags & LPM_STEP_TIME_NBODY) {
       cudaEvent_t e[2];
       LPM_CUDA(cudaEventCreate(&e[0]));
       LPM_CUDA(cudaEventCreate(&e[1]));
       LPM_CUDA(cudaEventRecord(e[0], ctx->stream));
-      lpm::launch_nbody(*ctx, plan, tgt, tself, src, part, eps);
+      lpm::launch_nbody(*ctx, pl, tgt, tself, src, part, eps);
       LPM_CUDA(cudaEventRecord(e[1], ctx->stream));
       timers.push_back(e[0]);
       timers.push_back(e[1]);
       return;
     }
-    lpm::launch_nbody(*ctx, plan, tgt, tself, src, part, eps);
+    lpm::launch_nbody(*ctx, pl, tgt, tself, src, part, eps);
   }
 
   std::vector<cudaEvent_t> timers;
@@ -344,7 +352,9 @@ struct lpm_ic2d_rk2 : lpm_stepper_base {
       if (T == 0) return;
       lpm::k_rk2_begin<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
       ctx->launches++;
-      nbody();
+      // the stage-1 stream function is overwritten by the final evaluation
+      // (as in Incompressible2DRK2::advance_timestep_impl), so it is not computed
+      nbody(false);
       lpm::k_rk2_mid<<<nb, 256, 0, ctx->stream>>>(g, k, b, P);
       ctx->launches++;
       nbody();
