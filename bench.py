@@ -323,6 +323,7 @@ def run_ours(args, rank, world, device):
             if not args.no_learned else None
         c5 = run_c5_leg(args, ctx, stream, device, run_learned_eval.weights) \
             if learned is not None and not args.no_c5 else None
+        other = run_other_legs(args, device) if not args.no_other else None
 
         # ---- accuracy 2: one RK4 step, FP32C vs the same algorithm in FP64
         # (chord form, LPM_FP64_CHORD), same flags; also its throughput ----
@@ -409,6 +410,7 @@ def run_ours(args, rank, world, device):
                 "one_rk4_step_vs_fp64_chord": step_err},
             "learned": learned,
             "c5_level8_far_field": c5,
+            "other_configurations": other,
             "cpu_baseline": cpu,
         }
     return result
@@ -429,17 +431,23 @@ def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
     from lpm_gb300.farfield import FarField
 
     theta = 0.4 if args.ff_theta is None else args.ff_theta
-    ff = FarField(theta=theta, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
+    # the network is trained on (cell, target) pairs with h/D in [rho_min,
+    # 0.5], the range of every setting used here and in the level-8 leg
+    trainer = FarField(theta=0.5, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
     t0 = time.perf_counter()
     if args.ff_weights:
         saved = np.load(args.ff_weights)
-        ff.set_weights(saved["w"], saved["norm"])
-        ff.set_network(True)
+        weights = (saved["w"], saved["norm"])
     else:
-        ff.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
-                 seed=20261203, level_min=5, level_max=8, eps=EPS)
+        trainer.train(nsamples=args.ff_samples, epochs=args.ff_epochs, batch=16384, lr=2e-3,
+                      seed=20261203, level_min=5, level_max=8, eps=EPS)
+        weights = trainer.get_weights()
     torch.cuda.synchronize(device)
     train_s = time.perf_counter() - t0
+    trainer.close()
+    ff = FarField(theta=theta, leaf_max=64, rho_min=args.ff_rho_min, ctx=ctx)
+    ff.set_weights(*weights)
+    ff.set_network(True)
     leaf = base.fm == 0
     xall = torch.cat([base.vx, base.fx[leaf]]).contiguous()
     u64 = torch.cat([s64.vu, s64.fu[leaf]])
@@ -478,7 +486,7 @@ def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
 
     ms_x = timed_steps(False)
     ms = timed_steps(True)
-    run_learned_eval.weights = ff.get_weights()
+    run_learned_eval.weights = weights
     return {"value": round(4 * ipe / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
             "ms_per_step": round(ms, 3), "theta": theta, "rho_min": args.ff_rho_min,
             "train_s": round(train_s, 2),
@@ -494,9 +502,28 @@ def run_learned_eval(args, ctx, stream, base, s64, ipe, device):
                     "fields of icosahedral levels 5-8"}
 
 
+def run_other_legs(args, device):
+    """Short runs of configurations C3 (planar dipoles, quad level 9) and C4
+    (256-problem ensemble) inside the default run: the same measurement as
+    --config c3 / c4 with 2 timed steps after 1 warm-up step."""
+    import copy
+
+    a = copy.copy(args)
+    a.steps, a.warmup = 2, 1
+    out = {}
+    for name, fn in (("c3_plane", run_plane), ("c4_ensemble", run_ensemble)):
+        r = fn(a, device)
+        keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config",
+                "roofline", "clocks", "gpu_launches", "errors_fp32c_vs_fp64_16384_vertex_targets")
+        out[name] = {k: r[k] for k in keep if k in r}
+    return out
+
+
 C5_SETTINGS = (  # (form, theta, rho_min): the configuration's setting first
-    ("learned", 0.5, 0.25), ("learned", 0.4, 0.30), ("learned", 0.35, 0.30),
+    ("learned", 0.5, 0.25), ("learned", 0.45, 0.25), ("learned", 0.4, 0.30),
+    ("learned", 0.35, 0.30),
     ("expansion_only", 0.4, None), ("expansion_only", 0.35, None), ("expansion_only", 0.3, None))
+NET_MODE = {"expansion_only": 0, "learned": 1}
 
 
 def run_c5_leg(args, ctx, stream, device, weights):
@@ -545,7 +572,7 @@ def run_c5_leg(args, ctx, stream, device, weights):
     for form, theta, rho in C5_SETTINGS:
         ff = FarField(theta=theta, leaf_max=64, rho_min=rho if rho else 0.25, ctx=ctx)
         ff.set_weights(*weights)
-        ff.set_network(form == "learned")
+        ff.set_network(NET_MODE[form])
         uall = torch.zeros_like(xall)
         ff.velocity(uall, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
         torch.cuda.synchronize(device)
@@ -569,12 +596,12 @@ def run_c5_leg(args, ctx, stream, device, weights):
         rows.append({"form": form, "theta": theta, "rho_min": rho,
                      "value": round(4 * ipe / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 2),
                      "error_vs_fp64": err, "network_rows": ff.stats().get("network_rows")
-                     if form == "learned" else 0})
+                     if form != "expansion_only" else 0})
         ff.close()
     spec = rows[0]
     ok = [r for r in rows if r["error_vs_fp64"]["linf"] <= 1e-4]
     best = {f: max((r for r in ok if r["form"] == f), key=lambda r: r["value"], default=None)
-            for f in ("learned", "expansion_only")}
+            for f in NET_MODE}
     return {"workload": "BVE sphere icosahedral level 8 RK4, Rossby-Haurwitz R=4, eps=0.01, "
                         "dt=0.005, octree far field (leaves <= 64, order-4 expansion)",
             "value": spec["value"], "unit": UNIT, "theta": spec["theta"],
@@ -787,7 +814,9 @@ def run_ensemble(args, device):
                                    "levels 3-6, 1-4 Gaussian vortices each, eps=0.01, dt=0.005",
                        "levels_histogram": {int(l): int((levels == l).sum()) for l in range(3, 7)},
                        "interactions_per_step": 4 * ipe, "chunk_len": info["chunk_len"],
-                       "kernel_shape": "%d threads x %d targets" % ens.shape(),
+                       "kernel_shape": "%d threads x %d targets, %s" % (
+                           ens.shape()[:2] + ("persistent" if ens.shape()[2]
+                                              else "one CTA per work item",)),
                        "work_items_per_evaluation": info["items"], "autotune_s": round(tune_s, 2)},
             "roofline": {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2),
                          "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
@@ -868,16 +897,20 @@ def run_c1(args, device):
 
 
 def c3_roofline(device, pairs_per_s: float) -> dict:
-    """Planar u + psi: 16 credited flops per pair against the FP32 FMA peak;
-    the pair needs two special-function results (reciprocal, log2), so the
-    XU pipe (16 per clock per SM) bounds it at 8 pairs per clock per SM."""
+    """Planar RK2 step: the stage evaluation computes the velocity only (13
+    credited flops per pair, one special-function result: the reciprocal),
+    the final evaluation velocity and stream function (16 flops, two:
+    reciprocal and log2); the stage's stream function would be overwritten.
+    Per pair of the step: 14.5 credited flops against the FP32 FMA peak; the
+    XU pipe (16 results per clock per SM) bounds the step at
+    2 / (1/16 + 1/8) = 10.7 pairs per clock per SM."""
     peak, sm_max, nsm = fp32_peak(device)
-    ach = pairs_per_s * 16 / 1e12
-    xu_pairs = 8 * nsm * sm_max * 1e6
+    ach = pairs_per_s * 14.5 / 1e12
+    xu_pairs = 2 / (1 / 16 + 1 / 8) * nsm * sm_max * 1e6
     return {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
             "frac": round(ach / peak, 4), "traffic": None,
-            "kernel": "nbody_chord<float,2,u,psi>, whole RK2 step timed",
-            "flops_per_pair_credited": 16,
+            "kernel": "nbody_chord<float,2,u> + nbody_chord<float,2,u,psi>, whole RK2 step timed",
+            "flops_per_pair_credited": 14.5,
             "xu_bound_pairs_per_s": xu_pairs, "frac_of_xu_bound": round(pairs_per_s / xu_pairs, 4),
             "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"}
 
@@ -956,8 +989,10 @@ def run_plane(args, device):
     """Configuration C3: planar incompressible flow, colliding Lamb dipoles of
     radius 1 and strength +-2 centred at (-+2, 0), uniform quad mesh of
     [-4, 4]^2 at level 9 (1024 x 1024 leaf cells), eps = 0.02, RK2 dt = 0.01;
-    velocity and stream function at every evaluation (FP32C).  Accuracy: FP32C
-    vs the reference FP64 arithmetic on 16,384 seeded vertex targets."""
+    velocity and stream function of every step (FP32C; the stage evaluation
+    computes the velocity only, its stream function being overwritten by the
+    final evaluation as in the reference).  Accuracy: FP32C vs the reference
+    FP64 arithmetic on 16,384 seeded vertex targets."""
     import torch
 
     from lpm_gb300 import build as B
@@ -1489,6 +1524,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true",
                     help="c2: skip the learned far-field evaluation")
+    ap.add_argument("--no-other", action="store_true",
+                    help="c2: skip the short C3 and C4 legs")
     ap.add_argument("--no-c5", action="store_true",
                     help="c2: skip the level-8 far-field leg (configuration C5)")
     ap.add_argument("--c5-steps", type=int, default=3,

@@ -293,8 +293,9 @@ int lpm_ic2d_rk2_step(lpm_ic2d_rk2* st, lpm_view vx, double* vzeta,
  * face slots (fixed).  precision: LPM_FP32C or LPM_FP64_CHORD (chord form,
  * velocity only).  Each evaluation is one persistent launch over (problem,
  * target block, source chunk) work items; a step is replayed from a CUDA
- * graph; the chunk length and the FP32 kernel shape (threads x targets per
- * thread) are autotuned on the first call. */
+ * graph; the chunk length, the FP32 kernel shape (threads x targets per
+ * thread) and the launch form (persistent or one CTA per item) are autotuned
+ * on the first call. */
 typedef struct lpm_ensemble lpm_ensemble;
 int lpm_ensemble_create(lpm_context* ctx, lpm_ensemble** out, int nproblems,
                         const int64_t* nverts, const int64_t* nfaces,
@@ -314,8 +315,16 @@ int lpm_ensemble_advance_timestep(lpm_ensemble* e, lpm_view vx, double* vzeta,
 int lpm_ensemble_info(lpm_ensemble* e, int64_t* chunk_len, int64_t* items,
                       int64_t* targets);
 int lpm_ensemble_nbody_time(lpm_ensemble* e, double* ms, int64_t* launches);
-/* Kernel shape in use: threads per CTA and targets per thread. */
-int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread);
+/* Kernel in use: threads per CTA, targets per thread and the launch form
+ * (persistent: 1 = persistent CTAs drain the work list, 0 = one CTA per work
+ * item, longest first; nullable). */
+int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread,
+                       int* persistent);
+/* Fixes the FP32 kernel shape (0-3: 256x4 with 3 or 4 CTAs per SM, 128x8,
+ * 256x2) and the launch form (persistent 1 or one CTA per item 0); with
+ * lpm_ensemble_set_chunk_len, instead of autotuning.  Results do not depend
+ * on either.  Call before the first velocity/step call. */
+int lpm_ensemble_set_kernel(lpm_ensemble* e, int shape, int persistent);
 /* Fixes the chunk length (sources; rounded up to whole tiles) instead of
  * autotuning it, e.g. for bitwise-reproducible runs across ensembles.  Call
  * before the first velocity/step call. */

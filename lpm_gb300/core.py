@@ -67,7 +67,7 @@ EXPORTS = [
     "lpm_swe_plane_face_sums", "lpm_swe_sphere_vertex_sums", "lpm_swe_sphere_face_sums",
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
-    "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape",
+    "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape", "lpm_ensemble_set_kernel",
     "lpm_netcdf_write_polymesh",
 ]
 
@@ -150,7 +150,8 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ensemble_velocity": [vp, V, V, V, vp, V, vp],
         "lpm_ensemble_advance_timestep": [vp, V, vp, V, V, vp, V, vp],
         "lpm_ensemble_info": [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)],
-        "lpm_ensemble_shape": [vp, C.POINTER(i32), C.POINTER(i32)],
+        "lpm_ensemble_shape": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
+        "lpm_ensemble_set_kernel": [vp, i32, i32],
         "lpm_ensemble_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_ensemble_set_chunk_len": [vp, i64],
         "lpm_sphere_tangency": [vp, vp, V, V, i64],

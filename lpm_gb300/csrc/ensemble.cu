@@ -1,5 +1,5 @@
 // ensemble.cu -- many independent BVE sphere problems of uneven size advanced
-// together: every evaluation is ONE persistent N-body launch over a work list
+// together: every evaluation is ONE N-body launch over a work list
 // of (problem, target block, source chunk) items, and a whole RK4 step (four
 // evaluations plus the fused stage epilogues) is captured once into a CUDA
 // graph and replayed.
@@ -12,9 +12,11 @@
 // sorted by decreasing chunk length, so the persistent CTAs drain it
 // longest-first and the tail stays short.  The chunk length and the FP32
 // kernel shape (threads x targets per thread, the kF32Shapes of the
-// single-problem kernel) are chosen by an autotuner that times one
-// evaluation per candidate at set-up: chunk lengths with the default shape,
-// then the shapes at the best length.  A target's sums do not depend on the
+// single-problem kernel) and the launch form (persistent CTAs draining the
+// list, or one CTA per item launched longest first) are chosen by an
+// autotuner that times one evaluation per candidate at set-up: chunk
+// lengths with the default shape in the persistent form, then every shape in
+// both forms at the best length.  A target's sums do not depend on the
 // shape (each target is summed by one thread in source order), so only the
 // chunk length changes results in the last bits.
 //
@@ -100,6 +102,57 @@ __global__ void __launch_bounds__(NT, MINB)
   }
 }
 
+// The same work items with one CTA each (item = blockIdx.x): the items are
+// ordered longest first, so the hardware's CTA scheduler drains them in that
+// order as resident slots free up.  The body is the persistent kernel's
+// without the item loop; the sums are the same bit for bit.
+template <typename T, int R, int NT, int TILE, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    ens_nbody_items(const int4* __restrict__ items,
+                    const typename Vec4<T>::type* __restrict__ tgt,
+                    const typename SrcRec<T>::type* __restrict__ src, const int64_t* ptoff,
+                    const int64_t* ptpad, const int64_t* psoff, const int64_t* pspad,
+                    const int64_t* ppart, int chunk_len, T c0, double* __restrict__ part,
+                    int* err) {
+  using V4 = typename Vec4<T>::type;
+  using Rec = typename SrcRec<T>::type;
+  constexpr int NC = 3;
+  __shared__ __align__(128) Rec sbuf[2 * TILE];
+  __shared__ __align__(8) uint64_t sbar[2];
+  const int tid = threadIdx.x;
+  const int4 w = items[blockIdx.x];  // (problem, target block, chunk, -)
+  const int p = w.x;
+  const int64_t tl = (int64_t)w.y * (NT * R);
+  const int64_t sl = (int64_t)w.z * chunk_len;
+  int64_t slen = pspad[p] - sl;
+  if (slen > chunk_len) slen = chunk_len;
+  TilePipe<Rec, TILE> pipe{sbuf, sbar, src + psoff[p] + sl, int(slen / TILE)};
+  pipe.start();
+  T tx[R], ty[R], tz[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const V4 t = tgt[ptoff[p] + tl + r * NT + tid];
+    tx[r] = t.x;
+    ty[r] = t.y;
+    tz[r] = t.z;
+  }
+  T S[NC][R], C[NC][R];
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      S[k][r] = T(0);
+      C[k][r] = T(0);
+    }
+  if (!chord_chunk<T, 3, true, false, false, R, TILE>(pipe, tx, ty, tz, S, C, c0, err)) return;
+  const int64_t tp = ptpad[p];
+  double* out = part + ppart[p] + (int64_t)w.z * NC * tp + tl;
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[k * tp + r * NT + tid] = (double)S[k][r] + (double)C[k][r];
+}
+
 // Packs the current state (positions, vorticity) for an evaluation and
 // records the evaluation positions.
 template <class TG, class PK>
@@ -143,6 +196,7 @@ struct lpm_ensemble {
   double* part = nullptr;
   double* buf = nullptr;  // xs[4] (3T each), zs[4] (T each), xw (3T)
   int shape = 0;         // FP32 kernel shape (index into kF32Shapes)
+  bool persistent = true;  // launch form: persistent CTAs or one CTA per item
   int occ_shape[lpm::kNumF32Shapes] = {};  // resident CTAs per SM, per shape
   // graph
   cudaStream_t cap_stream = nullptr;
@@ -378,6 +432,13 @@ struct lpm_ensemble {
 
   template <int R, int NT, int MINB>
   void launch_f32(int grid) {
+    if (!persistent) {
+      lpm::ens_nbody_items<float, R, NT, lpm::F32_TILE, MINB>
+          <<<unsigned(nitems), NT, 0, ctx->stream>>>(
+              items, static_cast<const float4*>(tgt), static_cast<const lpm::SrcF32*>(src),
+              d_toff, d_tpad, d_soff, d_spad, d_ppart, chunk_len, float(c0()), part, ctx->d_err);
+      return;
+    }
     lpm::ens_nbody<float, R, NT, lpm::F32_TILE, MINB><<<grid, NT, 0, ctx->stream>>>(
         items, int(nitems), counter, static_cast<const float4*>(tgt),
         static_cast<const lpm::SrcF32*>(src), d_toff, d_tpad, d_soff, d_spad, d_ppart,
@@ -508,8 +569,9 @@ struct lpm_ensemble {
       LPM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
       return ms;
     };
-    // chunk length with the default shape
+    // chunk length with the default shape and the persistent form
     shape = 0;
+    persistent = true;
     for (int len : cands) {
       plan(len);
       const float ms = time_plan();
@@ -518,23 +580,29 @@ struct lpm_ensemble {
         best_len = len;
       }
     }
-    // kernel shape at that chunk length
+    // kernel shape and launch form at that chunk length
     int best_shape = 0;
+    bool best_persistent = true;
     if (f32()) {
-      for (int k = 1; k < lpm::kNumF32Shapes; ++k) {
-        shape = k;
-        plan(best_len);
-        const float ms = time_plan();
-        if (ms < best) {
-          best = ms;
-          best_shape = k;
+      for (int form = 0; form < 2; ++form)
+        for (int k = 0; k < lpm::kNumF32Shapes; ++k) {
+          if (form == 0 && k == 0) continue;  // timed above
+          shape = k;
+          persistent = form == 0;
+          plan(best_len);
+          const float ms = time_plan();
+          if (ms < best) {
+            best = ms;
+            best_shape = k;
+            best_persistent = persistent;
+          }
         }
-      }
     }
     flags = saved;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     shape = best_shape;
+    persistent = best_persistent;
     plan(best_len);
     tuned_ms = best;
   }
@@ -647,8 +715,10 @@ int lpm_ensemble_info(lpm_ensemble* e, int64_t* chunk_len, int64_t* items,
   return LPM_OK;
 }
 
-int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread) {
+int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread,
+                       int* persistent) {
   if (!e || !threads || !targets_per_thread) return lpm::fail(LPM_ERR_ARG, "null argument");
+  if (persistent) *persistent = e->persistent ? 1 : 0;
   if (e->f32()) {
     *threads = lpm::kF32Shapes[e->shape].nt;
     *targets_per_thread = lpm::kF32Shapes[e->shape].r;
@@ -656,6 +726,16 @@ int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread) {
     *threads = lpm::F64_NT;
     *targets_per_thread = lpm::F64_R;
   }
+  return LPM_OK;
+}
+
+int lpm_ensemble_set_kernel(lpm_ensemble* e, int shape, int persistent) {
+  if (!e || shape < 0 || shape >= lpm::kNumF32Shapes)
+    return lpm::fail(LPM_ERR_ARG, "lpm_ensemble_set_kernel: bad argument");
+  if (e->chunk_len != 0)
+    return lpm::fail(LPM_ERR_STATE, "lpm_ensemble_set_kernel: plan already chosen");
+  e->shape = e->f32() ? shape : 0;
+  e->persistent = e->f32() ? persistent != 0 : true;
   return LPM_OK;
 }
 

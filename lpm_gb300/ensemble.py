@@ -83,10 +83,16 @@ class BVEEnsemble:
         return {"chunk_len": a.value, "items": b.value, "targets": c.value}
 
     def shape(self):
-        """(threads per CTA, targets per thread) of the N-body kernel in use."""
-        a, b = C.c_int(), C.c_int()
-        check(lib().lpm_ensemble_shape(self._h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+        """(threads per CTA, targets per thread, persistent) of the N-body
+        kernel in use."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().lpm_ensemble_shape(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, bool(c.value)
+
+    def set_kernel(self, shape: int, persistent: bool):
+        """Fixes the kernel shape (index 0-3) and launch form (before the
+        first evaluation, together with set_chunk_len)."""
+        check(lib().lpm_ensemble_set_kernel(self._h, int(shape), int(bool(persistent))))
 
     def set_chunk_len(self, n: int):
         check(lib().lpm_ensemble_set_chunk_len(self._h, int(n)))

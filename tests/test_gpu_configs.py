@@ -17,8 +17,9 @@ result is checked on a seeded sample of targets against all sources.
   ic2d_dt_conv  tests/lpm_ic2d_tests.cpp:165-188 on the GPU stepper: cubed
       sphere depth 4, eps = 0, t_f = 0.5, steps {15, 30, 60}, the finest as
       the reference solution, rates > 1.95 in l1, l2 and linf.
-  C4  the ensemble (one persistent launch for all problems) against the
-      oracle directly, per problem, after one evaluation and two RK4 steps.
+  C4  the ensemble (one N-body launch per evaluation for all problems, in
+      the kernel form its autotuner chose) against the oracle directly, per
+      problem, after one evaluation and two RK4 steps.
 """
 import math
 

@@ -73,3 +73,26 @@ def test_ensemble_graph_replay_is_deterministic(gpu_ctx):
         ctx.synchronize()
         outs.append((ens.fx.clone(), ens.fvel.clone()))
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+def test_ensemble_kernel_forms_agree(gpu_ctx):
+    """Every kernel shape, persistent or one CTA per work item, gives the
+    same velocities bit for bit at a fixed chunk length."""
+    ctx = gpu_ctx
+    rng = np.random.default_rng(3)
+    levels = [3, 1, 4, 2]
+    params = [random_vortex_params(rng) for _ in levels]
+    outs = []
+    for shape in range(4):
+        for persistent in (True, False):
+            ens = BVEEnsemble(levels, params, 0.005, eps=0.01, flags=core.STEP_SKIP_MASKED_TARGETS,
+                              ctx=ctx)
+            ens.set_kernel(shape, persistent)
+            ens.set_chunk_len(2048)
+            ens.velocity()
+            ctx.synchronize()
+            assert ens.shape()[2] == persistent
+            outs.append((ens.vvel.clone(), ens.fvel.clone()))
+            ens.close()
+    for o in outs[1:]:
+        assert torch.equal(outs[0][0], o[0]) and torch.equal(outs[0][1], o[1])
