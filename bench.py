@@ -522,7 +522,8 @@ def run_other_legs(args, device):
 C5_SETTINGS = (  # (form, theta, rho_min): the configuration's setting first
     ("learned", 0.5, 0.25), ("learned", 0.45, 0.25), ("learned", 0.4, 0.30),
     ("learned", 0.35, 0.30),
-    ("expansion_only", 0.4, None), ("expansion_only", 0.35, None), ("expansion_only", 0.3, None))
+    ("expansion_only", 0.5, None), ("expansion_only", 0.4, None), ("expansion_only", 0.35, None),
+    ("expansion_only", 0.3, None))
 NET_MODE = {"expansion_only": 0, "learned": 1}
 
 
@@ -761,8 +762,9 @@ def run_ensemble(args, device):
     """Configuration C4: 256 independent BVE problems, icosahedral levels 3-6
     drawn uniformly from a seed, 1-4 Gaussian vortices each (centres uniform
     on the sphere, amplitudes U[pi, 4 pi], widths U[0.1, 0.4]), eps = 0.01,
-    RK4 dt = 0.005, FP32C; one persistent N-body launch per evaluation, RK4
-    steps replayed from a captured graph, chunk length autotuned."""
+    RK4 dt = 0.005, FP32C; one N-body launch per evaluation, RK4 steps
+    replayed from a captured graph, chunk length, kernel shape and launch form
+    autotuned (or fixed by --ens-plan)."""
     import torch
 
     from lpm_gb300 import build as B
@@ -779,8 +781,12 @@ def run_ensemble(args, device):
     params = [random_vortex_params(rng) for _ in levels]
     flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
     ens = BVEEnsemble(levels, params, DT, eps=EPS, precision=core.FP32C, flags=flags, ctx=ctx)
+    if args.ens_plan:  # a fixed plan: chunk length, shape index, persistent (0/1)
+        chunk, shape, persistent = (int(v) for v in args.ens_plan.split(","))
+        ens.set_kernel(shape, bool(persistent))
+        ens.set_chunk_len(chunk)
     t0 = time.perf_counter()
-    ens.velocity()  # autotunes the chunk length
+    ens.velocity()  # autotunes chunk length, kernel shape and launch form
     torch.cuda.synchronize(device)
     tune_s = time.perf_counter() - t0
     ipe = ens.interactions_per_evaluation()
@@ -820,7 +826,8 @@ def run_ensemble(args, device):
                        "work_items_per_evaluation": info["items"], "autotune_s": round(tune_s, 2)},
             "roofline": {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2),
                          "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
-                         "kernel": "ensemble N-body (persistent), whole RK4 step timed",
+                         "kernel": "ensemble N-body (%s), whole RK4 step timed" % (
+                             "persistent" if ens.shape()[2] else "one CTA per work item"),
                          "flops_per_pair_credited": FLOPS_PER_PAIR,
                          "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"},
             "clocks": clocks, "gpu_launches": launches}
@@ -1005,6 +1012,8 @@ def run_plane(args, device):
     ctx = core.Context(device)
     stream = torch.cuda.current_stream(device)
     ctx.set_stream(stream)
+    if args.fp32_shape is not None:  # else the stepper times the four shapes once
+        ctx.set_kernel_shape(args.fp32_shape)
     ic = Incompressible2D(core.MESH_QUAD_RECT, args.plane_level, radius=4.0, eps=0.02, ctx=ctx)
     ic.init_vorticity(core.IC_DIPOLE_PAIR, colliding_dipoles_params())
     ctx.set_precision(core.FP32C)
@@ -1519,7 +1528,11 @@ def main():
     ap.add_argument("--ff-weights", default=None,
                     help="c5: load a saved network instead of training")
     ap.add_argument("--plane-level", type=int, default=9)
+    ap.add_argument("--fp32-shape", type=int, default=None, choices=range(4),
+                    help="c3: fixed FP32 kernel shape instead of the per-size autotuner")
     ap.add_argument("--problems", type=int, default=256)
+    ap.add_argument("--ens-plan", default=None,
+                    help="c4: fixed plan 'chunk_len,shape,persistent' instead of the autotuner")
     ap.add_argument("--cpu-targets", type=int, default=16384)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-learned", action="store_true",

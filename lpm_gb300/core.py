@@ -68,7 +68,7 @@ EXPORTS = [
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
     "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape", "lpm_ensemble_set_kernel",
-    "lpm_netcdf_write_polymesh",
+    "lpm_netcdf_write_polymesh", "lpm_context_set_kernel_shape",
 ]
 
 
@@ -114,6 +114,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_context_destroy": [vp],
         "lpm_context_set_stream": [vp, vp],
         "lpm_context_set_precision": [vp, i32],
+        "lpm_context_set_kernel_shape": [vp, i32],
         "lpm_context_synchronize": [vp],
         "lpm_wait_selftest": [vp, i32],
         "lpm_context_kernel_launches": [vp],
@@ -244,6 +245,11 @@ class Context:
     def set_precision(self, precision: int) -> None:
         check(lib().lpm_context_set_precision(self._h, precision))
         self.precision = precision
+
+    def set_kernel_shape(self, shape: int) -> None:
+        """Fixes the FP32 N-body kernel shape (0-3) of later LPM_FP32C sums,
+        or -1 for per-size autotuning (the default)."""
+        check(lib().lpm_context_set_kernel_shape(self._h, int(shape)))
 
     def set_stream(self, stream) -> None:
         """stream: a torch.cuda.Stream, or an integer cudaStream_t."""

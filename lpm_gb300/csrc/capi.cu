@@ -7,6 +7,7 @@
 #include <string>
 
 #include "lpm_host.hpp"
+#include "nbody.cuh"
 
 namespace lpm {
 
@@ -215,6 +216,14 @@ int lpm_context_set_precision(lpm_context* ctx, int precision) {
                 "precision must be LPM_FP64 (64), LPM_FP64_CHORD (65), LPM_FP64_EXACT (66) "
                 "or LPM_FP32C (32)");
   ctx->precision = precision;
+  return LPM_OK;
+}
+
+int lpm_context_set_kernel_shape(lpm_context* ctx, int shape) {
+  if (!ctx) return fail(LPM_ERR_ARG, "null context");
+  if (shape < -1 || shape >= lpm::kNumF32Shapes)
+    return fail(LPM_ERR_ARG, "lpm_context_set_kernel_shape: shape must be -1 or 0-3");
+  ctx->forced_shape = shape;
   return LPM_OK;
 }
 

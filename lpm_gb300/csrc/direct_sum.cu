@@ -453,6 +453,7 @@ void launch_nbody(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
 int tune_shape(lpm_context& ctx, const NbodyPlan& p0, const void* tgt, const int* tself,
                const void* src, double* part, double eps) {
   if (p0.precision != LPM_FP32C) return 0;
+  if (ctx.forced_shape >= 0) return ctx.forced_shape;
   auto lg = [](int64_t v) {
     int k = 0;
     while ((int64_t(1) << k) < v) ++k;

@@ -121,6 +121,7 @@ struct lpm_context {
   size_t max_part_bytes = 0;  // cap on chunk-partial scratch (0 = none)
   std::map<uint64_t, int> tuned;  // autotuned FP32 kernel shape per size class
   bool autotune = true;
+  int forced_shape = -1;  // >= 0: FP32 kernel shape fixed by the caller
 };
 
 namespace lpm {
