@@ -217,6 +217,44 @@ def test_determinism(gpu_ctx):
         assert same(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("geom,eps", [("sphere", 0.01), ("plane", 0.02), ("plane", 0.0)])
+def test_fp32_kernel_shapes_agree(gpu_ctx, oracle, geom, eps):
+    """Every FP32 kernel shape gives the same bits (each target is summed by
+    one thread in source order, with the same operations whatever the
+    shape), and each is within the FP32C tolerance of the oracle."""
+    ctx = gpu_ctx
+    ctx.set_precision(core.FP32C)
+    if geom == "sphere":
+        vx, fx, fa, fm, zf = sphere_case(4)
+    else:
+        vx, fx, fa, fm = core.build_mesh(core.MESH_QUAD_RECT, 5, 4.0)
+        zf = core.eval_ic(core.IC_DIPOLE_PAIR, (2.0, 1.0, -2.0, 0.0, -2.0, 1.0, 2.0, 0.0), fx)
+    nd = vx.shape[1]
+    dvx, dfx, dz, da, dm = dev(vx), dev(fx), dev(zf), dev(fa), dev(fm)
+    outs = []
+    try:
+        for shape in range(4):
+            ctx.set_kernel_shape(shape)
+            u = torch.zeros(vx.shape[0], nd, dtype=torch.float64, device="cuda")
+            p = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
+            F.ic2d_passive_sums(ctx, u, p, dvx, dfx, dz, da, dm, eps)
+            outs.append((u, p))
+        ctx.synchronize()
+    finally:
+        ctx.set_kernel_shape(-1)
+    for u, p in outs[1:]:
+        assert same(u, outs[0][0]) and same(p, outs[0][1])
+    oracle.set_sphere_form(True)
+    try:
+        u_p, psi_p = oracle.ic2d_passive_sums(vx, fx, zf, fa, fm, eps)
+    finally:
+        oracle.set_sphere_form(False)
+    assert rel(outs[0][0].cpu(), u_p) < TOL32
+    assert rel(outs[0][1].cpu(), psi_p) < TOL32
+    with pytest.raises(core.LpmError):
+        ctx.set_kernel_shape(4)
+
+
 def test_argument_errors(gpu_ctx):
     ctx = gpu_ctx
     L = core.lib()
