@@ -905,24 +905,23 @@ def run_c1(args, device):
 
 def c3_roofline(device, pairs_per_s: float) -> dict:
     """Planar RK2 step: the stage evaluation computes the velocity only (13
-    credited flops per pair), the final evaluation velocity and stream
-    function (16 flops); the stage's stream function would be overwritten.
+    credited flops per pair, one special-function result: the reciprocal),
+    the final evaluation velocity and stream function (16 flops, two:
+    reciprocal and log2); the stage's stream function would be overwritten.
     Per pair of the step: 14.5 credited flops against the FP32 FMA peak.
-    Pipe bound of the executed work: the stage pair is 7 FP32-pipe lane
-    operations (packed f32x2) and one MUFU reciprocal, the final pair 8 and
-    two (reciprocal, log2); at 128 FP32 lanes and 32 MUFU results per clock
-    per SM (the FP32 sphere kernel's MUFU instructions run at 31.6 % of the
-    XU pipe's peak while its FMA pipe is 79 % busy) that is
-    min(128/7, 32) = 18.3 and min(128/8, 32/2) = 16 pairs per clock per SM,
-    2 / (1/18.3 + 1/16) = 17.1 for the step."""
+    The XU pipe bounds the step: it delivers 16 MUFU results per clock per
+    SM (each reciprocal or log2 holds it two cycles: ncu shows the final
+    kernel's XU pipe 94.5 % busy at 47.9 % of its instruction peak), so
+    16 pairs per clock per SM in the stage and 8 in the final evaluation,
+    2 / (1/16 + 1/8) = 10.7 for the step."""
     peak, sm_max, nsm = fp32_peak(device)
     ach = pairs_per_s * 14.5 / 1e12
-    bound = 2 / (7 / 128 + 8 / 128) * nsm * sm_max * 1e6
+    xu_pairs = 2 / (1 / 16 + 1 / 8) * nsm * sm_max * 1e6
     return {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
             "frac": round(ach / peak, 4), "traffic": None,
             "kernel": "nbody_chord<float,2,u> + nbody_chord<float,2,u,psi>, whole RK2 step timed",
             "flops_per_pair_credited": 14.5,
-            "pipe_bound_pairs_per_s": bound, "frac_of_pipe_bound": round(pairs_per_s / bound, 4),
+            "xu_bound_pairs_per_s": xu_pairs, "frac_of_xu_bound": round(pairs_per_s / xu_pairs, 4),
             "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz"}
 
 
