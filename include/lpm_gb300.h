@@ -87,10 +87,12 @@ int lpm_context_set_stream(lpm_context* ctx, void* cuda_stream);
 /* LPM_FP64 (default), LPM_FP64_EXACT, LPM_FP64_CHORD or LPM_FP32C for the
  * functor entry points below. */
 int lpm_context_set_precision(lpm_context* ctx, int precision);
-/* Fixes the FP32 N-body kernel shape of later LPM_FP32C sums (0-3: 256x4
- * with 3 or 4 CTAs per SM, 128x8, 256x2, as for lpm_ensemble_set_kernel), or
- * (-1, the default) lets each problem size time the four shapes once and keep
- * the fastest.  A target's sums do not depend on the shape. */
+/* Fixes the FP32 N-body kernel shape (0-3: 256x4 with 3 or 4 CTAs per SM,
+ * 128x8, 256x2, as for lpm_ensemble_set_kernel) of later LPM_FP32C functor
+ * calls and of steppers created afterwards (a stepper keeps the shape it was
+ * created with), or (-1, the default) lets each problem size time the four
+ * shapes once and keep the fastest.  A target's sums do not depend on the
+ * shape. */
 int lpm_context_set_kernel_shape(lpm_context* ctx, int shape);
 /* Waits for the context's stream, then reports LPM_ERR_TIMEOUT if a bounded
  * device-side wait gave up since the last check (and clears the flag). */

@@ -14,6 +14,8 @@ result is checked on a seeded sample of targets against all sources.
       FP64 1e-12, FP32C 1e-6.
   C3  quad level 9 on [-4, 4]^2, colliding dipoles, eps = 0.02: 2,048 seeded
       targets, FP64 1e-12, FP32C 1e-6 (velocity) and 2e-6 (stream function).
+  L9  icosahedral level 9 sources (5.2 M) for 4,096 seeded targets, FP64
+      1e-12, FP32C 1e-6: the largest index ranges of the suite.
   ic2d_dt_conv  tests/lpm_ic2d_tests.cpp:165-188 on the GPU stepper: cubed
       sphere depth 4, eps = 0, t_f = 0.5, steps {15, 30, 60}, the finest as
       the reference solution, rates > 1.95 in l1, l2 and linf.
@@ -139,6 +141,35 @@ def test_c3_quad9_sample(gpu_ctx, oracle, precision, tol, tolp):
     assert np.array_equal(ru[1024:], ra) and np.array_equal(rp[1024:], rpa)
     assert rel(u.cpu(), ru) < tol
     assert rel(p.cpu(), rp) < tolp
+
+
+@pytest.fixture(scope="module")
+def level9(oracle):
+    """Icosahedral level 9 (5,242,880 leaf sources in 6,990,500 face slots),
+    the C2 initial condition, 2,048 seeded vertices and 2,048 seeded leaf
+    centres as passive targets, and the oracle's FP64 velocity there."""
+    eps = 0.01
+    vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 9)
+    fz = O.ic_eval(O.IC_GAUSSIAN_SPHERE, (4 * math.pi, 4.0, 0.0, 0.05 * math.pi, 0.0, OMEGA), fx)
+    iv = sample(vx.shape[0], 2048, 5)
+    jf = sample(fx.shape[0], 2048, 6, fm == 0)
+    tx = np.concatenate([vx[iv], fx[jf]])
+    ru, _ = oracle.ic2d_passive_sums(tx, fx, fz, fa, fm, eps, want_psi=False)
+    return tx, fx, fz, fa, fm, eps, ru
+
+
+@pytest.mark.parametrize("precision,tol", [(core.FP64, 1e-12), (core.FP32C, 1e-6)])
+def test_level9_sources(gpu_ctx, level9, precision, tol):
+    """The largest source set of the tests: 5.2 M sources (10,240 FP32 tiles,
+    hundreds of chunks), so chunk counts, partial offsets and source indices
+    run well past the other cases' ranges."""
+    ctx = gpu_ctx
+    ctx.set_precision(precision)
+    tx, fx, fz, fa, fm, eps, ru = level9
+    u = zeros(tx.shape[0], 3)
+    F.ic2d_passive_sums(ctx, u, None, dev(tx), dev(fx), dev(fz), dev(fa), dev(fm), eps)
+    ctx.synchronize()
+    assert rel(u.cpu(), ru) < tol
 
 
 def test_ic2d_dt_conv(gpu_ctx):
