@@ -49,7 +49,7 @@ def test_solid_body_rotation(gpu_ctx, precision):
     ctx.set_precision(precision)
     eu, ep = [], []
     for level in (4, 5, 6):
-        vx, psi, u = vertex_solve(ctx, level, core.IC_SOLID_BODY, ())
+        vx, psi, u = vertex_solve(ctx, level, O.IC_SOLID_BODY, ())
         exact = np.stack([-OMEGA * vx[:, 1], OMEGA * vx[:, 0], 0 * vx[:, 0]], 1)
         eu.append(linf(u, exact))
         ep.append(linf(psi, 2 * math.pi * vx[:, 2]))
@@ -65,7 +65,7 @@ def test_rossby_haurwitz_analytic_velocity(gpu_ctx, precision):
     w = OMEGA / 12.5
     errs = []
     for level in (4, 5, 6):
-        vx, _, u = vertex_solve(ctx, level, core.IC_RH54, (w, -w))
+        vx, _, u = vertex_solve(ctx, level, O.IC_RH54, (w, -w))
         lat, lon = np.arcsin(vx[:, 2]), np.arctan2(vx[:, 1], vx[:, 0])
         amp, u0 = -w, w
         uu = amp * 0.5 * np.cos(4 * lon) * np.cos(lat) ** 3 * (5 * np.cos(2 * lat) - 3)
@@ -82,7 +82,7 @@ def test_tangency(gpu_ctx, precision, tol):
     ctx = gpu_ctx
     ctx.set_precision(precision)
     vx, fx, fa, fm = O.mesh(O.MESH_ICOS_TRI, 5, 1.0)
-    zf = O.ic_eval(core.IC_SOLID_BODY, (), fx) + np.random.default_rng(1).standard_normal(fx.shape[0])
+    zf = O.ic_eval(O.IC_SOLID_BODY, (), fx) + np.random.default_rng(1).standard_normal(fx.shape[0])
     u = torch.zeros(vx.shape[0], 3, dtype=torch.float64, device="cuda")
     F.bve_vertex_velocity(ctx, u, dev(vx), dev(fx), dev(zf), dev(fa), dev(fm))
     ctx.synchronize()
