@@ -39,6 +39,12 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dd(double a, double b) { return __ddiv_rn(a, b); }
 
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+  u64 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 constexpr int kSweNT = 128;   // targets per CTA
 constexpr int kSweTile = 256;  // sources per shared-memory tile
 constexpr int kSweNC = 9;
@@ -168,39 +174,123 @@ __global__ void k_swe_out(const double* __restrict__ part, int nchunks, int64_t 
 // kernel uses |d|^2 directly (the reference's sqrt then square is the
 // identity).  Positions and surface heights are split into FP32 hi + lo parts
 // (d and s_y - s_x are small differences of O(1) values).  Three MUFU
-// results (reciprocal, log2, exp2) and ~45 FP32 instructions per pair.
+// results (reciprocal, log2, exp2) and ~45 FP32 operations per pair, two
+// sources per packed f32x2 instruction (pair k holds sources 2k, 2k + 1; an
+// odd count ends with a zero-strength, zero-area source), the sums kept per
+// lane over a 256-source tile and then merged by TwoSum.
 constexpr int kPl32NC = 15;
 
-struct __align__(16) PlSrc32 {
-  float4 p;  // x hi, y hi, x lo, y lo
-  float4 w;  // rot, pot, area, surface hi
-  float4 e;  // surface lo, slot (int bits), -, -
+struct __align__(16) PlPair32 {
+  float4 hxy;  // x hi of sources 2k, 2k + 1; y hi
+  float4 lxy;  // x lo; y lo
+  float4 rp;   // rot; pot
+  float4 as;   // area; surface hi
+  float4 sl;   // surface lo; slot (int bits)
 };
 
 __global__ void k_swe_plane32_pack(View fx, const double* __restrict__ zeta,
                                    const double* __restrict__ sigma,
                                    const double* __restrict__ area, const double* __restrict__ sfc,
                                    const int* __restrict__ src2slot, int64_t ns,
-                                   PlSrc32* __restrict__ src) {
+                                   PlPair32* __restrict__ src) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (k >= ns) return;
-  const int64_t j = src2slot[k];
-  const double x = fx(j, 0), y = fx(j, 1), sv = sfc[j];
-  const float xh = float(x), yh = float(y), sh = float(sv);
-  PlSrc32 r;
-  r.p = make_float4(xh, yh, float(x - xh), float(y - yh));
-  r.w = make_float4(float(zeta[j] * area[j]), float(sigma[j] * area[j]), float(area[j]), sh);
-  r.e = make_float4(float(sv - sh), __int_as_float(int(j)), 0.f, 0.f);
+  if (k >= (ns + 1) / 2) return;
+  float v[2][9] = {};
+  int sl[2] = {-1, -1};
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    if (2 * k + e >= ns) break;
+    const int64_t j = src2slot[2 * k + e];
+    const double x = fx(j, 0), y = fx(j, 1), sv = sfc[j];
+    const float xh = float(x), yh = float(y), sh = float(sv);
+    v[e][0] = xh;
+    v[e][1] = yh;
+    v[e][2] = float(x - xh);
+    v[e][3] = float(y - yh);
+    v[e][4] = float(zeta[j] * area[j]);
+    v[e][5] = float(sigma[j] * area[j]);
+    v[e][6] = float(area[j]);
+    v[e][7] = sh;
+    v[e][8] = float(sv - sh);
+    sl[e] = int(j);
+  }
+  PlPair32 r;
+  r.hxy = make_float4(v[0][0], v[1][0], v[0][1], v[1][1]);
+  r.lxy = make_float4(v[0][2], v[1][2], v[0][3], v[1][3]);
+  r.rp = make_float4(v[0][4], v[1][4], v[0][5], v[1][5]);
+  r.as = make_float4(v[0][6], v[1][6], v[0][7], v[1][7]);
+  r.sl = make_float4(v[0][8], v[1][8], __int_as_float(sl[0]), __int_as_float(sl[1]));
   src[k] = r;
+}
+
+// One pair record against one target.  COLL: face targets; the source in the
+// target's own slot is skipped (its reciprocal and logarithm are replaced by
+// 0, and its PSE term is 0: d = 0 and s_y - s_x = 0).  TAIL: the record may
+// hold the zero-strength dummy (slot -1, at the origin, which can coincide
+// with a target), whose reciprocal and logarithm are zeroed the same way.
+struct Pl32Target {
+  u64 x0h, x1h, sh, x0l, x1l, sl, e2, ipse2;
+  int64_t i;
+};
+
+template <bool COLL, bool TAIL>
+__device__ __forceinline__ void pl32_pair(const PlPair32& s, const Pl32Target& t,
+                                          u64 (&w)[kPl32NC]) {
+  const u64 d0 = add2(sub2(t.x0h, pk2(s.hxy.x, s.hxy.y)), sub2(t.x0l, pk2(s.lxy.x, s.lxy.y)));
+  const u64 d1 = add2(sub2(t.x1h, pk2(s.hxy.z, s.hxy.w)), sub2(t.x1l, pk2(s.lxy.z, s.lxy.w)));
+  const u64 dd = fma2(d0, d0, mul2(d1, d1));
+  float qa, qb;
+  upk2(add2(dd, t.e2), qa, qb);
+  float ra = rcp_approx(qa), rb = rcp_approx(qb);
+  float la = lg2_approx(qa), lb = lg2_approx(qb);
+  if (COLL || TAIL) {
+    const int sa = __float_as_int(s.sl.z), sb = __float_as_int(s.sl.w);
+    const bool ska = (COLL && sa == t.i) || (TAIL && sa < 0);
+    const bool skb = (COLL && sb == t.i) || (TAIL && sb < 0);
+    ra = ska ? 0.f : ra;
+    la = ska ? 0.f : la;
+    rb = skb ? 0.f : rb;
+    lb = skb ? 0.f : lb;
+  }
+  const u64 r = pk2(ra, rb), L = pk2(la, lb);
+  const u64 p2 = mul2(dd, t.ipse2);
+  float ea, eb;
+  upk2(mul2(p2, pk2(-1.4426950408889634f, -1.4426950408889634f)), ea, eb);
+  float xa, xb;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(xa) : "f"(ea));
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(xb) : "f"(eb));
+  const u64 poly = fma2(fma2(fma2(pk2(-2.f / 3.f, -2.f / 3.f), p2, pk2(10.f, 10.f)), p2,
+                             pk2(-40.f, -40.f)),
+                        p2, pk2(40.f, 40.f));
+  const u64 ds = add2(sub2(pk2(s.as.z, s.as.w), t.sh), sub2(pk2(s.sl.x, s.sl.y), t.sl));
+  const u64 rot = pk2(s.rp.x, s.rp.y), pot = pk2(s.rp.z, s.rp.w);
+  const u64 a = mul2(rot, r), b = mul2(pot, r);
+  const u64 a2 = mul2(a, r), b2 = mul2(b, r);
+  w[0] = fma2(a, d0, w[0]);
+  w[1] = fma2(a, d1, w[1]);
+  w[2] = fma2(b, d0, w[2]);
+  w[3] = fma2(b, d1, w[3]);
+  w[4] = add2(w[4], a);
+  w[5] = add2(w[5], b);
+  const u64 ad0 = mul2(a2, d0), ad1 = mul2(a2, d1), bd0 = mul2(b2, d0), bd1 = mul2(b2, d1);
+  w[6] = fma2(ad0, d0, w[6]);
+  w[7] = fma2(ad0, d1, w[7]);
+  w[8] = fma2(ad1, d1, w[8]);
+  w[9] = fma2(bd0, d0, w[9]);
+  w[10] = fma2(bd0, d1, w[10]);
+  w[11] = fma2(bd1, d1, w[11]);
+  w[12] = fma2(mul2(ds, pk2(s.as.x, s.as.y)), mul2(poly, pk2(xa, xb)), w[12]);
+  w[13] = fma2(rot, L, w[13]);
+  w[14] = fma2(pot, L, w[14]);
 }
 
 template <bool COLL>
 __global__ void __launch_bounds__(kSweNT) k_swe_plane32(View tx, const double* __restrict__ ts,
-                                                        int64_t nt, const PlSrc32* __restrict__ src,
+                                                        int64_t nt, const PlPair32* __restrict__ src,
                                                         int64_t ns, int64_t chunk_len, float e2,
                                                         float ipse2, double* __restrict__ part,
                                                         int64_t tpad) {
-  __shared__ PlSrc32 tile[kSweTile];
+  __shared__ PlPair32 tile[kSweTile / 2];
   const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
   const int64_t c = blockIdx.y;
   const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
@@ -209,55 +299,31 @@ __global__ void __launch_bounds__(kSweNT) k_swe_plane32(View tx, const double* _
   const double SX = valid ? ts[i] : 0.0;
   const float x0h = float(X0), x1h = float(X1), sxh = float(SX);
   const float x0l = float(X0 - x0h), x1l = float(X1 - x1h), sxl = float(SX - sxh);
-  const float kLog2e = 1.4426950408889634f;
+  const Pl32Target t{pk2(x0h, x0h), pk2(x1h, x1h), pk2(sxh, sxh), pk2(x0l, x0l),
+                     pk2(x1l, x1l), pk2(sxl, sxl), pk2(e2, e2),  pk2(ipse2, ipse2), i};
   float S[kPl32NC], C[kPl32NC];
 #pragma unroll
   for (int k = 0; k < kPl32NC; ++k) S[k] = C[k] = 0.f;
-  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {  // t0 is even: chunks are whole tiles
     const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    const int mp = (m + 1) / 2;
     __syncthreads();
-    for (int q = threadIdx.x; q < m; q += kSweNT) tile[q] = src[t0 + q];
+    for (int q = threadIdx.x; q < mp; q += kSweNT) tile[q] = src[t0 / 2 + q];
     __syncthreads();
     if (!valid) continue;
-    float w[kPl32NC];
+    u64 w[kPl32NC];
 #pragma unroll
-    for (int k = 0; k < kPl32NC; ++k) w[k] = 0.f;
+    for (int k = 0; k < kPl32NC; ++k) w[k] = 0ull;
 #pragma unroll 2
-    for (int q = 0; q < m; ++q) {
-      const float4 P = tile[q].p, W = tile[q].w, E = tile[q].e;
-      if (COLL && __float_as_int(E.y) == i) continue;
-      const float d0 = (x0h - P.x) + (x0l - P.z);
-      const float d1 = (x1h - P.y) + (x1l - P.w);
-      const float dd = fmaf(d0, d0, d1 * d1);
-      const float R = dd + e2;
-      const float r = rcp_approx(R);
-      const float L = lg2_approx(R);
-      const float p2 = dd * ipse2;
-      float ex;
-      asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(ex) : "f"(-p2 * kLog2e));
-      const float poly = fmaf(fmaf(fmaf(-2.f / 3.f, p2, 10.f), p2, -40.f), p2, 40.f);
-      const float ds = (W.w - sxh) + (E.x - sxl);
-      const float a = W.x * r, b = W.y * r;
-      const float a2 = a * r, b2 = b * r;
-      w[0] = fmaf(a, d0, w[0]);
-      w[1] = fmaf(a, d1, w[1]);
-      w[2] = fmaf(b, d0, w[2]);
-      w[3] = fmaf(b, d1, w[3]);
-      w[4] += a;
-      w[5] += b;
-      const float ad0 = a2 * d0, ad1 = a2 * d1, bd0 = b2 * d0, bd1 = b2 * d1;
-      w[6] = fmaf(ad0, d0, w[6]);
-      w[7] = fmaf(ad0, d1, w[7]);
-      w[8] = fmaf(ad1, d1, w[8]);
-      w[9] = fmaf(bd0, d0, w[9]);
-      w[10] = fmaf(bd0, d1, w[10]);
-      w[11] = fmaf(bd1, d1, w[11]);
-      w[12] = fmaf(ds * W.z, poly * ex, w[12]);
-      w[13] = fmaf(W.x, L, w[13]);
-      w[14] = fmaf(W.y, L, w[14]);
-    }
+    for (int q = 0; q < m / 2; ++q) pl32_pair<COLL, false>(tile[q], t, w);
+    if (m & 1) pl32_pair<COLL, true>(tile[mp - 1], t, w);  // the dummy's pair
 #pragma unroll
-    for (int k = 0; k < kPl32NC; ++k) two_sum_acc(S[k], C[k], w[k]);
+    for (int k = 0; k < kPl32NC; ++k) {
+      float a, b;
+      upk2(w[k], a, b);
+      two_sum_acc(S[k], C[k], a);
+      two_sum_acc(S[k], C[k], b);
+    }
   }
   if (!valid) return;
 #pragma unroll
@@ -468,115 +534,156 @@ __global__ void k_swe_sphere_out(const double* __restrict__ part, int nchunks, i
 //       + [Z x - A]x - (G - H/2) P.
 // Positions are split into FP32 hi + lo parts so that d = (xh - yh) +
 // (xl - yl) carries its own FP32 rounding, not the positions' (near pairs
-// dominate the gradient: their |d| shrinks with the mesh).  Per-pair work is
-// FP32 with one MUFU reciprocal (~50 instructions); each 256-source tile's FP32
-// partials are merged into (sum, compensation) pairs by TwoSum.
+// dominate the gradient: their |d| shrinks with the mesh).  Per pair: 52 FP32
+// operations and one MUFU reciprocal.  Two sources per packed f32x2
+// instruction: pair k of the packed array holds sources 2k and 2k + 1 (an odd
+// count ends with a zero-strength source at the origin, whose terms are
+// exactly 0), each thread owns one target, and the 27 sums are kept per lane
+// (even and odd sources) over a 256-source tile; the two lanes' tile
+// partials are then added into FP64 running sums in shared memory (which
+// frees the registers the packed sums need).
 constexpr int kSph32NC = 27;  // A3 B3 U1[3] V1[3] U2[6] V2[6] Z G H
 
-struct __align__(16) SphSrc32 {
-  float4 hi;  // x, y, z, rot / (2 pi)
-  float4 lo;  // x - hi.x, y - hi.y, z - hi.z, pot / (2 pi)
+struct __align__(16) SphPair32 {
+  float4 hxy;  // x hi of sources 2k, 2k + 1; y hi of 2k, 2k + 1
+  float4 hzr;  // z hi; rot / (2 pi)
+  float4 lxy;  // x lo (x - x hi); y lo
+  float4 lzp;  // z lo; pot / (2 pi)
 };
 
 __global__ void k_swe_sphere32_pack(View fx, const double* __restrict__ zeta,
                                     const double* __restrict__ sigma,
                                     const double* __restrict__ area,
                                     const int* __restrict__ src2slot, int64_t ns,
-                                    SphSrc32* __restrict__ src, int* __restrict__ slot) {
+                                    SphPair32* __restrict__ src, int2* __restrict__ slot) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  if (k >= ns) return;
-  const int64_t j = src2slot[k];
-  const double x = fx(j, 0), y = fx(j, 1), z = fx(j, 2);
-  const float xh = float(x), yh = float(y), zh = float(z);
+  if (k >= (ns + 1) / 2) return;
   const double inv2pi = 1.0 / (2 * kPI);
-  SphSrc32 r;
-  r.hi = make_float4(xh, yh, zh, float(-zeta[j] * area[j] * inv2pi));
-  r.lo = make_float4(float(x - xh), float(y - yh), float(z - zh), float(-sigma[j] * area[j] * inv2pi));
+  float h[2][4] = {}, l[2][4] = {};
+  int sl[2] = {-1, -1};
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    if (2 * k + e >= ns) break;
+    const int64_t j = src2slot[2 * k + e];
+    const double x = fx(j, 0), y = fx(j, 1), z = fx(j, 2);
+    h[e][0] = float(x);
+    h[e][1] = float(y);
+    h[e][2] = float(z);
+    h[e][3] = float(-zeta[j] * area[j] * inv2pi);
+    l[e][0] = float(x - double(h[e][0]));
+    l[e][1] = float(y - double(h[e][1]));
+    l[e][2] = float(z - double(h[e][2]));
+    l[e][3] = float(-sigma[j] * area[j] * inv2pi);
+    sl[e] = int(j);
+  }
+  SphPair32 r;
+  r.hxy = make_float4(h[0][0], h[1][0], h[0][1], h[1][1]);
+  r.hzr = make_float4(h[0][2], h[1][2], h[0][3], h[1][3]);
+  r.lxy = make_float4(l[0][0], l[1][0], l[0][1], l[1][1]);
+  r.lzp = make_float4(l[0][2], l[1][2], l[0][3], l[1][3]);
   src[k] = r;
-  slot[k] = int(j);
+  slot[k] = make_int2(sl[0], sl[1]);
 }
 
+// COLL: face targets; the source in the target's own slot is skipped (its
+// reciprocal is replaced by 0, which zeroes every term of the pair).
 template <bool COLL>
-__global__ void __launch_bounds__(kSweNT) k_swe_sphere32(View tx, int64_t nt,
-                                                         const SphSrc32* __restrict__ src,
-                                                         const int* __restrict__ slot, int64_t ns,
-                                                         int64_t chunk_len, float c0,
-                                                         double* __restrict__ part, int64_t tpad) {
-  __shared__ SphSrc32 tile[kSweTile];
-  __shared__ int tslot[COLL ? kSweTile : 1];
-  const int64_t i = blockIdx.x * int64_t(kSweNT) + threadIdx.x;
+__global__ void __launch_bounds__(kSweNT, 4) k_swe_sphere32(View tx, int64_t nt,
+                                                            const SphPair32* __restrict__ src,
+                                                            const int2* __restrict__ slot,
+                                                            int64_t ns, int64_t chunk_len, float c0,
+                                                            double* __restrict__ part,
+                                                            int64_t tpad) {
+  __shared__ SphPair32 tile[kSweTile / 2];
+  __shared__ int2 tslot[COLL ? kSweTile / 2 : 1];
+  __shared__ double acc[kSph32NC][kSweNT];
+  const int tid = threadIdx.x;
+  const int64_t i = blockIdx.x * int64_t(kSweNT) + tid;
   const int64_t c = blockIdx.y;
   const int64_t j0 = c * chunk_len, j1 = ns < j0 + chunk_len ? ns : j0 + chunk_len;
   const bool valid = i < nt;
-  float xh[3], xl[3];
+  u64 XH[3], XL[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const double v = valid ? tx(i, a) : 0.0;
-    xh[a] = float(v);
-    xl[a] = float(v - double(xh[a]));
+    const float h = float(v), l = float(v - double(h));
+    XH[a] = pk2(h, h);
+    XL[a] = pk2(l, l);
   }
-  float S[kSph32NC], C[kSph32NC];
+  const u64 C02 = pk2(c0, c0);
 #pragma unroll
-  for (int k = 0; k < kSph32NC; ++k) S[k] = C[k] = 0.f;
-  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {
+  for (int k = 0; k < kSph32NC; ++k) acc[k][tid] = 0.0;
+  for (int64_t t0 = j0; t0 < j1; t0 += kSweTile) {  // t0 is even: chunks are whole tiles
     const int m = int(j1 - t0 < kSweTile ? j1 - t0 : kSweTile);
+    const int mp = (m + 1) / 2;
     __syncthreads();
-    for (int q = threadIdx.x; q < m; q += kSweNT) {
-      tile[q] = src[t0 + q];
-      if (COLL) tslot[q] = slot[t0 + q];
+    for (int q = tid; q < mp; q += kSweNT) {
+      tile[q] = src[t0 / 2 + q];
+      if (COLL) tslot[q] = slot[t0 / 2 + q];
     }
     __syncthreads();
     if (!valid) continue;
-    float w[kSph32NC];
+    u64 w[kSph32NC];
 #pragma unroll
-    for (int k = 0; k < kSph32NC; ++k) w[k] = 0.f;
+    for (int k = 0; k < kSph32NC; ++k) w[k] = 0ull;
 #pragma unroll 2
-    for (int q = 0; q < m; ++q) {
-      if (COLL && tslot[q] == i) continue;
-      const float4 h = tile[q].hi, l = tile[q].lo;
-      const float d0 = (xh[0] - h.x) + (xl[0] - l.x);
-      const float d1 = (xh[1] - h.y) + (xl[1] - l.y);
-      const float d2 = (xh[2] - h.z) + (xl[2] - l.z);
-      const float dd = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
-      const float r = rcp_approx(dd + c0);
-      const float sz = h.w * r, ss = l.w * r;
-      const float R = (sz + sz) * r, Q = (ss + ss) * r;
-      w[0] = fmaf(sz, d0, w[0]);
-      w[1] = fmaf(sz, d1, w[1]);
-      w[2] = fmaf(sz, d2, w[2]);
-      w[3] = fmaf(ss, d0, w[3]);
-      w[4] = fmaf(ss, d1, w[4]);
-      w[5] = fmaf(ss, d2, w[5]);
-      const float r0 = R * d0, r1 = R * d1, r2 = R * d2;
-      const float q0 = Q * d0, q1 = Q * d1, q2 = Q * d2;
-      w[6] += r0;
-      w[7] += r1;
-      w[8] += r2;
-      w[9] += q0;
-      w[10] += q1;
-      w[11] += q2;
-      w[12] = fmaf(r0, d0, w[12]);
-      w[13] = fmaf(r0, d1, w[13]);
-      w[14] = fmaf(r0, d2, w[14]);
-      w[15] = fmaf(r1, d1, w[15]);
-      w[16] = fmaf(r1, d2, w[16]);
-      w[17] = fmaf(r2, d2, w[17]);
-      w[18] = fmaf(q0, d0, w[18]);
-      w[19] = fmaf(q0, d1, w[19]);
-      w[20] = fmaf(q0, d2, w[20]);
-      w[21] = fmaf(q1, d1, w[21]);
-      w[22] = fmaf(q1, d2, w[22]);
-      w[23] = fmaf(q2, d2, w[23]);
-      w[24] += sz;
-      w[25] += ss;
-      w[26] = fmaf(ss, dd, w[26]);
+    for (int q = 0; q < mp; ++q) {
+      const SphPair32 s = tile[q];
+      const u64 d0 = add2(sub2(XH[0], pk2(s.hxy.x, s.hxy.y)), sub2(XL[0], pk2(s.lxy.x, s.lxy.y)));
+      const u64 d1 = add2(sub2(XH[1], pk2(s.hxy.z, s.hxy.w)), sub2(XL[1], pk2(s.lxy.z, s.lxy.w)));
+      const u64 d2 = add2(sub2(XH[2], pk2(s.hzr.x, s.hzr.y)), sub2(XL[2], pk2(s.lzp.x, s.lzp.y)));
+      const u64 dd = fma2(d0, d0, fma2(d1, d1, mul2(d2, d2)));
+      float qa, qb;
+      upk2(add2(dd, C02), qa, qb);
+      float ra = rcp_approx(qa), rb = rcp_approx(qb);
+      if (COLL) {
+        const int2 sl = tslot[q];
+        ra = sl.x == i ? 0.f : ra;
+        rb = sl.y == i ? 0.f : rb;
+      }
+      const u64 r = pk2(ra, rb);
+      const u64 sz = mul2(pk2(s.hzr.z, s.hzr.w), r), ss = mul2(pk2(s.lzp.z, s.lzp.w), r);
+      const u64 R = mul2(add2(sz, sz), r), Q = mul2(add2(ss, ss), r);
+      w[0] = fma2(sz, d0, w[0]);
+      w[1] = fma2(sz, d1, w[1]);
+      w[2] = fma2(sz, d2, w[2]);
+      w[3] = fma2(ss, d0, w[3]);
+      w[4] = fma2(ss, d1, w[4]);
+      w[5] = fma2(ss, d2, w[5]);
+      const u64 r0 = mul2(R, d0), r1 = mul2(R, d1), r2 = mul2(R, d2);
+      const u64 q0 = mul2(Q, d0), q1 = mul2(Q, d1), q2 = mul2(Q, d2);
+      w[6] = add2(w[6], r0);
+      w[7] = add2(w[7], r1);
+      w[8] = add2(w[8], r2);
+      w[9] = add2(w[9], q0);
+      w[10] = add2(w[10], q1);
+      w[11] = add2(w[11], q2);
+      w[12] = fma2(r0, d0, w[12]);
+      w[13] = fma2(r0, d1, w[13]);
+      w[14] = fma2(r0, d2, w[14]);
+      w[15] = fma2(r1, d1, w[15]);
+      w[16] = fma2(r1, d2, w[16]);
+      w[17] = fma2(r2, d2, w[17]);
+      w[18] = fma2(q0, d0, w[18]);
+      w[19] = fma2(q0, d1, w[19]);
+      w[20] = fma2(q0, d2, w[20]);
+      w[21] = fma2(q1, d1, w[21]);
+      w[22] = fma2(q1, d2, w[22]);
+      w[23] = fma2(q2, d2, w[23]);
+      w[24] = add2(w[24], sz);
+      w[25] = add2(w[25], ss);
+      w[26] = fma2(ss, dd, w[26]);
     }
 #pragma unroll
-    for (int k = 0; k < kSph32NC; ++k) two_sum_acc(S[k], C[k], w[k]);
+    for (int k = 0; k < kSph32NC; ++k) {
+      float a, b;
+      upk2(w[k], a, b);
+      acc[k][tid] += double(a) + double(b);
+    }
   }
   if (!valid) return;
 #pragma unroll
-  for (int k = 0; k < kSph32NC; ++k) part[(c * kSph32NC + k) * tpad + i] = double(S[k]) + double(C[k]);
+  for (int k = 0; k < kSph32NC; ++k) part[(c * kSph32NC + k) * tpad + i] = acc[k][tid];
 }
 
 __global__ void k_swe_sphere32_out(const double* __restrict__ part, int nchunks, int64_t tpad,
@@ -674,8 +781,9 @@ SwePlan swe_plan(lpm_context& ctx, const uint8_t* mask, int64_t nt, int64_t nf, 
   int* slot2src = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
   p.src2slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(nf, 1)));
   p.ns = compact_sources(ctx, mask, nf, slot2src, p.src2slot);
-  p.src = ctx.arena.take(rec_bytes * std::max<int64_t>(p.ns, 1));
-  if (want_slot) p.slot = static_cast<int*>(ctx.arena.take(sizeof(int) * std::max<int64_t>(p.ns, 1)));
+  // one record more than the sources: the FP32 spherical path packs pairs
+  p.src = ctx.arena.take(rec_bytes * size_t(p.ns + 1));
+  if (want_slot) p.slot = static_cast<int*>(ctx.arena.take(sizeof(int) * size_t(p.ns + 1)));
   int64_t len = (p.ns + nch_max - 1) / nch_max;
   p.chunk_len = std::max<int64_t>(kSweTile, (len + kSweTile - 1) / kSweTile * kSweTile);
   p.nchunks = int(std::max<int64_t>(1, (p.ns + p.chunk_len - 1) / p.chunk_len));
@@ -689,19 +797,22 @@ void swe_sphere_sums32(lpm_context& ctx, View tx, int64_t nt, View fx, const dou
                        const double* sigma, const double* area, const uint8_t* mask, int64_t nf,
                        double eps, bool collocated, View u, double* ddot, double* grad,
                        int do_velocity) {
-  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(SphSrc32), kSph32NC, true);
-  auto* src = static_cast<SphSrc32*>(p.src);
+  // one 64-byte pair record per two sources (32 bytes per source, plus one
+  // dummy for an odd count); the pair slots take the plan's slot array
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(SphPair32) / 2, kSph32NC, true);
+  auto* src = static_cast<SphPair32*>(p.src);
+  auto* pslot = reinterpret_cast<int2*>(p.slot);
   if (p.ns > 0) {
-    k_swe_sphere32_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area,
-                                                                 p.src2slot, p.ns, src, p.slot);
+    k_swe_sphere32_pack<<<blocks256((p.ns + 1) / 2), 256, 0, ctx.stream>>>(
+        fx, zeta, sigma, area, p.src2slot, p.ns, src, pslot);
     ctx.launches++;
   }
   const float c0 = float(2 * eps * eps);
   if (collocated)
-    k_swe_sphere32<true><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, p.slot, p.ns,
+    k_swe_sphere32<true><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, pslot, p.ns,
                                                               p.chunk_len, c0, p.part, p.tpad);
   else
-    k_swe_sphere32<false><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, p.slot, p.ns,
+    k_swe_sphere32<false><<<p.grid(), kSweNT, 0, ctx.stream>>>(tx, nt, src, pslot, p.ns,
                                                                p.chunk_len, c0, p.part, p.tpad);
   k_swe_sphere32_out<<<blocks256(nt), 256, 0, ctx.stream>>>(p.part, p.nchunks, p.tpad, tx, nt,
                                                             eps * eps, u, ddot, grad, do_velocity);
@@ -747,11 +858,12 @@ void swe_plane_sums32(lpm_context& ctx, View tx, const double* ts, int64_t nt, V
                       const double* zeta, const double* sigma, const double* area,
                       const uint8_t* mask, const double* sfc, int64_t nf, double eps,
                       double pse_eps, bool collocated, const SweOut& out) {
-  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(PlSrc32), kPl32NC, false);
-  auto* src = static_cast<PlSrc32*>(p.src);
+  // one 80-byte pair record per two sources (plus one dummy for an odd count)
+  const SwePlan p = swe_plan(ctx, mask, nt, nf, sizeof(PlPair32) / 2, kPl32NC, false);
+  auto* src = static_cast<PlPair32*>(p.src);
   if (p.ns > 0) {
-    k_swe_plane32_pack<<<blocks256(p.ns), 256, 0, ctx.stream>>>(fx, zeta, sigma, area, sfc,
-                                                                p.src2slot, p.ns, src);
+    k_swe_plane32_pack<<<blocks256((p.ns + 1) / 2), 256, 0, ctx.stream>>>(
+        fx, zeta, sigma, area, sfc, p.src2slot, p.ns, src);
     ctx.launches++;
   }
   const float e2 = float(eps * eps), ipse2 = float(1.0 / (pse_eps * pse_eps));

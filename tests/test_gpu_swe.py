@@ -315,3 +315,62 @@ def test_swe_plane_fp32c_views_and_flags():
                               T["fs"], 0.05, 0.3)
     torch.cuda.synchronize()
     assert not bool(z["u"].any()) and not bool(z["psi"].any())
+
+
+@pytest.mark.parametrize("eps", [0.0, 0.05])
+def test_swe_fp32c_odd_source_count(oracle, eps):
+    """The FP32C kernels take their sources two at a time; with an odd count
+    the last pair carries a zero-strength dummy at the origin.  One leaf more
+    is masked here so the count is odd, and the quad mesh has a vertex at the
+    origin (with eps = 0 the dummy coincides with that target): both forms
+    stay within their tolerances of the FP64 oracle."""
+    import torch
+
+    from lpm_gb300 import core
+    from lpm_gb300 import functors as F
+
+    ctx = core.Context(0, precision=core.FP32C)
+    d = torch.device("cuda", 0)
+    # plane
+    vx, fx, fa, fm, zeta, sigma, fs, vs = _fields(4)
+    fm = fm.copy()
+    fm[np.flatnonzero(fm == 0)[7]] = 1
+    assert (fm == 0).sum() % 2 == 1 and np.any(np.all(vx == 0, axis=1))
+    pse_eps = math.sqrt(fa[fm == 0].mean()) ** 0.55
+    T = {k: torch.tensor(v, device=d) for k, v in
+         dict(vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, sg=sigma, fs=fs, vs=vs).items()}
+    gv = F.swe_plane_vertex_sums(ctx, T["vx"], T["vs"], T["fx"], T["z"], T["sg"], T["fa"],
+                                 T["fm"], T["fs"], eps, pse_eps)
+    gf = F.swe_plane_face_sums(ctx, T["fx"], T["z"], T["sg"], T["fa"], T["fm"], T["fs"], eps,
+                               pse_eps)
+    torch.cuda.synchronize()
+    rv = oracle.swe_plane_sums(vx, vs, fx, zeta, sigma, fa, fm, fs, eps, pse_eps, collocated=False)
+    rf = oracle.swe_plane_sums(fx, fs, fx, zeta, sigma, fa, fm, fs, eps, pse_eps,
+                               collocated=not eps > 0)
+    tol = {"u": 1e-6, "psi": 3e-6, "phi": 3e-6, "du1dx1": 3e-5, "du1dx2": 3e-5, "du2dx1": 3e-5,
+           "du2dx2": 3e-5, "laps": 3e-5}
+    leaf = fm == 0
+    for got, ref, sel in ((gv, rv, slice(None)), (gf, rf, leaf)):
+        cols = {"u": ref[:, 0:2], "du1dx1": ref[:, 2], "du1dx2": ref[:, 3], "du2dx1": ref[:, 4],
+                "du2dx2": ref[:, 5], "laps": ref[:, 6], "psi": ref[:, 7], "phi": ref[:, 8]}
+        for k, t in tol.items():
+            g = got[k].cpu().numpy()[sel]
+            assert np.isfinite(g).all(), k
+            assert _rel(g, cols[k][sel]) < t, k
+    # sphere
+    vx, fx, fa, fm, zeta, sigma = _sphere_fields(4)
+    fm = fm.copy()
+    fm[np.flatnonzero(fm == 0)[7]] = 1
+    assert (fm == 0).sum() % 2 == 1
+    T = _dev(ctx, vx=vx, fx=fx, fa=fa, fm=fm, z=zeta, s=sigma)
+    gv = F.swe_sphere_vertex_sums(ctx, T["vx"], T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                  want_grad=True)
+    gf = F.swe_sphere_face_sums(ctx, T["fx"], T["z"], T["s"], T["fa"], T["fm"], eps,
+                                want_grad=True)
+    torch.cuda.synchronize()
+    rv = oracle.swe_sphere_sums(vx, fx, zeta, sigma, fa, fm, eps)
+    rf = oracle.swe_sphere_sums(fx, fx, zeta, sigma, fa, fm, eps, collocated=eps == 0)
+    leaf = fm == 0
+    for got, ref, sel in ((gv, rv, slice(None)), (gf, rf, leaf)):
+        assert _rel(got["u"].cpu().numpy()[sel], ref[sel, :3]) < 1e-6
+        assert _rel(got["grad"].cpu().numpy()[sel], ref[sel, 3:]) < 2e-5
