@@ -1333,7 +1333,7 @@ def run_c5(args, device):
     ctx = core.Context(device)
     stream = torch.cuda.current_stream(device)
     ctx.set_stream(stream)
-    L = args.level if args.level != LEVEL else 8
+    L = args.c5_level
     t0 = time.perf_counter()
     vx, fx, fa, fm = core.build_mesh(core.MESH_ICOS_TRI, L, 1.0)
     mesh_host_s = time.perf_counter() - t0
@@ -1544,6 +1544,8 @@ def main():
                     help="c2: skip the short C3 and C4 legs")
     ap.add_argument("--no-c5", action="store_true",
                     help="c2: skip the level-8 far-field leg (configuration C5)")
+    ap.add_argument("--c5-level", type=int, default=8,
+                    help="c5: icosahedral level (the configuration's is 8)")
     ap.add_argument("--c5-steps", type=int, default=3,
                     help="c2: timed RK4 steps per far-field setting of the level-8 leg")
     ap.add_argument("--only-headline", action="store_true",
