@@ -534,8 +534,10 @@ __global__ void k_swe_sphere_out(const double* __restrict__ part, int nchunks, i
 //       + [Z x - A]x - (G - H/2) P.
 // Positions are split into FP32 hi + lo parts so that d = (xh - yh) +
 // (xl - yl) carries its own FP32 rounding, not the positions' (near pairs
-// dominate the gradient: their |d| shrinks with the mesh).  Per pair: 52 FP32
-// operations and one MUFU reciprocal.  Two sources per packed f32x2
+// dominate the gradient: their |d| shrinks with the mesh).  Per pair: 50 FP32
+// operations and one MUFU reciprocal (the strengths are stored doubled, as
+// rot, pot / pi, so that R, Q = sz r, ss r need no doubling; the epilogue
+// halves the sums of sz and ss, exactly).  Two sources per packed f32x2
 // instruction: pair k of the packed array holds sources 2k and 2k + 1 (an odd
 // count ends with a zero-strength source at the origin, whose terms are
 // exactly 0), each thread owns one target, and the 27 sums are kept per lane
@@ -558,7 +560,7 @@ __global__ void k_swe_sphere32_pack(View fx, const double* __restrict__ zeta,
                                     SphPair32* __restrict__ src, int2* __restrict__ slot) {
   const int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
   if (k >= (ns + 1) / 2) return;
-  const double inv2pi = 1.0 / (2 * kPI);
+  const double inv_pi = 1.0 / kPI;  // strengths stored doubled: rot, pot / pi
   float h[2][4] = {}, l[2][4] = {};
   int sl[2] = {-1, -1};
 #pragma unroll
@@ -569,11 +571,11 @@ __global__ void k_swe_sphere32_pack(View fx, const double* __restrict__ zeta,
     h[e][0] = float(x);
     h[e][1] = float(y);
     h[e][2] = float(z);
-    h[e][3] = float(-zeta[j] * area[j] * inv2pi);
+    h[e][3] = float(-zeta[j] * area[j] * inv_pi);
     l[e][0] = float(x - double(h[e][0]));
     l[e][1] = float(y - double(h[e][1]));
     l[e][2] = float(z - double(h[e][2]));
-    l[e][3] = float(-sigma[j] * area[j] * inv2pi);
+    l[e][3] = float(-sigma[j] * area[j] * inv_pi);
     sl[e] = int(j);
   }
   SphPair32 r;
@@ -642,8 +644,10 @@ __global__ void __launch_bounds__(kSweNT, 4) k_swe_sphere32(View tx, int64_t nt,
         rb = sl.y == i ? 0.f : rb;
       }
       const u64 r = pk2(ra, rb);
+      // sz, ss are twice the pair scalars (the strengths are stored doubled),
+      // so R, Q = sz r, ss r; the sums of sz and ss are halved in the epilogue
       const u64 sz = mul2(pk2(s.hzr.z, s.hzr.w), r), ss = mul2(pk2(s.lzp.z, s.lzp.w), r);
-      const u64 R = mul2(add2(sz, sz), r), Q = mul2(add2(ss, ss), r);
+      const u64 R = mul2(sz, r), Q = mul2(ss, r);
       w[0] = fma2(sz, d0, w[0]);
       w[1] = fma2(sz, d1, w[1]);
       w[2] = fma2(sz, d2, w[2]);
@@ -698,6 +702,9 @@ __global__ void k_swe_sphere32_out(const double* __restrict__ part, int nchunks,
   for (int c = 0; c < nchunks; ++c)
 #pragma unroll
     for (int k = 0; k < kSph32NC; ++k) s[k] += part[(int64_t(c) * kSph32NC + k) * tpad + i];
+  // the kernel's sz, ss were doubled (strengths stored as rot, pot / pi):
+  // halve A, B, Z, G, H (exact)
+  for (int k : {0, 1, 2, 3, 4, 5, 24, 25, 26}) s[k] *= 0.5;
   const double x[3] = {tx(i, 0), tx(i, 1), tx(i, 2)};
   const double *A = s, *B = s + 3, *U1 = s + 6, *V1 = s + 9;
   const int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};  // (a, b) -> packed symmetric index
