@@ -37,6 +37,7 @@
 
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 
 #include <cuda_runtime.h>
 
@@ -226,6 +227,86 @@ __device__ __forceinline__ void two_sum_acc(double& s, double& c, double p) {
   c += e;
 }
 
+// Which sources (bit k: source index = k mod 8) take their reciprocal from
+// Newton's method on the FMA pipe instead of the MUFU: the planar kernel with
+// velocity and stream function needs two MUFU results per pair (reciprocal,
+// log2), and a MUFU result holds the XU pipe two cycles (16 per clock per SM),
+// while the pair's 8 FP32 lane operations leave half of the FP32 pipe (128
+// lanes per clock per SM) idle.  The Newton reciprocal costs 6 FP32 lane
+// operations (3 packed FMAs) and one integer operation; with 4 sources in 8
+// both pipes bound the loop at ~10.7 pairs per clock per SM instead of 8.
+// The choice depends on the source's index alone (tiles and chunks start at
+// multiples of 8), so a target's sums do not depend on the kernel shape or the
+// chunking.  The velocity-only kernels keep the MUFU for every source.
+__host__ __device__ constexpr unsigned soft_rcp_sources(int ndim, bool wu, bool wp) {
+  return (ndim == 2 && wu && wp) ? 0x55u : 0u;
+}
+
+// -1/q for a packed pair of positive normal floats, by Newton's method on the
+// negated reciprocal y (y <- y + y (1 + q y), two FMAs, no negation) from the
+// bit-level initial approximation -1/q ~ bits(0xFEF311C3 - bits(q)) (the
+// classic integer reciprocal seed, relative error <= 5.1 %): three steps take
+// it to <= 0.5 ulp (6e-8 relative), tested against FP64 1/q.
+__device__ __forceinline__ u64 neg_rcp2(u64 q, float qa, float qb, u64 one2) {
+  u64 y = pk2(__uint_as_float(0xFEF311C3u - __float_as_uint(qa)),
+              __uint_as_float(0xFEF311C3u - __float_as_uint(qb)));
+#pragma unroll
+  for (int it = 0; it < 3; ++it) y = fma2(y, fma2(q, y, one2), y);
+  return y;
+}
+
+// One source record against the thread's H packed target pairs (FP32 chord
+// form, velocity and stream function); SOFT: the reciprocal by neg_rcp2.
+template <bool SOFT, int NDIM, bool SKIPC, int H, int NC, typename Rec>
+__device__ __forceinline__ void chord_pair_up(const Rec& s, const u64 (&TX)[H], const u64 (&TY)[H],
+                                              const u64 (&TZ)[H], u64 C02, float c0, u64 one2,
+                                              u64 (&P)[NC][H]) {
+  const u64 sx = pk2(s.a.x, s.a.y), sy = pk2(s.a.z, s.a.w);
+  const u64 sz = pk2(s.b.x, s.b.y), sw = pk2(s.b.z, s.b.w);
+  u64 nsw = 0ull;
+  if constexpr (SOFT) nsw = fma2(sw, pk2(-1.f, -1.f), 0ull);  // -g, exact
+#pragma unroll
+  for (int h = 0; h < H; ++h) {
+    const u64 dx = sub2(TX[h], sx);
+    const u64 dy = sub2(TY[h], sy);
+    u64 dz = 0ull;
+    u64 q;
+    if (NDIM == 3) {
+      dz = sub2(TZ[h], sz);
+      q = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, C02)));
+    } else {
+      q = fma2(dx, dx, fma2(dy, dy, C02));
+    }
+    float qa, qb;
+    upk2(q, qa, qb);
+    u64 w;
+    if constexpr (SOFT)
+      w = mul2(nsw, neg_rcp2(q, qa, qb, one2));
+    else
+      w = mul2(sw, pk2(rcp_approx(qa), rcp_approx(qb)));
+    P[0][h] = fma2(w, dx, P[0][h]);
+    P[1][h] = fma2(w, dy, P[1][h]);
+    if (NDIM == 3) P[2][h] = fma2(w, dz, P[2][h]);
+    float la = lg2_approx(qa), lb = lg2_approx(qb);
+    if (SKIPC) {
+      la = (qa == c0) ? 0.f : la;
+      lb = (qb == c0) ? 0.f : lb;
+    }
+    P[NC - 1][h] = fma2(sw, pk2(la, lb), P[NC - 1][h]);
+  }
+}
+
+// Eight consecutive sources, each with its compile-time reciprocal choice.
+template <unsigned PAT, int NDIM, bool SKIPC, int H, int NC, typename Rec, size_t... J>
+__device__ __forceinline__ void chord_group8_up(const Rec* sm, const u64 (&TX)[H],
+                                                const u64 (&TY)[H], const u64 (&TZ)[H], u64 C02,
+                                                float c0, u64 one2, u64 (&P)[NC][H],
+                                                std::index_sequence<J...>) {
+  (chord_pair_up<((PAT >> J) & 1u) != 0, NDIM, SKIPC, H, NC>(sm[J], TX, TY, TZ, C02, c0, one2,
+                                                             P),
+   ...);
+}
+
 // SKIPC: in the stream-function sum, drop coincident pairs (q == c0, i.e.
 // d == 0: the skipped i == j term).  The velocity term of such a pair is 0.
 template <typename T, int NDIM, bool WU, bool WP>
@@ -271,6 +352,15 @@ __device__ __forceinline__ bool chord_chunk(
 #pragma unroll
         for (int h = 0; h < H; ++h) P[k][h] = 0ull;
 
+      constexpr unsigned kSoft = soft_rcp_sources(NDIM, WU, WP);
+      if constexpr (kSoft != 0) {
+        static_assert(TILE % 8 == 0, "the soft-reciprocal pattern repeats every 8 sources");
+        const u64 one2 = pk2(1.f, 1.f);
+#pragma unroll 1
+        for (int j0 = 0; j0 < TILE; j0 += 8)
+          chord_group8_up<kSoft, NDIM, SKIPC, H, NC>(sm + j0, TX, TY, TZ, C02, c0, one2, P,
+                                                     std::make_index_sequence<8>{});
+      } else {
 #pragma unroll 4
       for (int j = 0; j < TILE; ++j) {
         const Rec s = sm[j];
@@ -305,6 +395,7 @@ __device__ __forceinline__ bool chord_chunk(
             P[NC - 1][h] = fma2(sw, pk2(la, lb), P[NC - 1][h]);
           }
         }
+      }
       }
 #pragma unroll
       for (int k = 0; k < NC; ++k)
