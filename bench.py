@@ -906,17 +906,21 @@ def run_c1(args, device):
 def c3_roofline(device, pairs_per_s: float) -> dict:
     """Planar RK2 step: the stage evaluation computes the velocity only (13
     credited flops per pair, one special-function result: the reciprocal),
-    the final evaluation velocity and stream function (16 flops, two:
-    reciprocal and log2); the stage's stream function would be overwritten.
-    Per pair of the step: 14.5 credited flops against the FP32 FMA peak.
-    The XU pipe bounds the step: it delivers 16 MUFU results per clock per
-    SM (each reciprocal or log2 holds it two cycles: ncu shows the final
-    kernel's XU pipe 94.5 % busy at 47.9 % of its instruction peak), so
-    16 pairs per clock per SM in the stage and 8 in the final evaluation,
-    2 / (1/16 + 1/8) = 10.7 for the step."""
+    the final evaluation velocity and stream function (16 flops; the
+    logarithm from the MUFU, the reciprocal from the MUFU for 5 sources in 8
+    and from Newton's method on the FMA pipe for the other 3: soft_rcp_sources
+    in lpm_gb300/csrc/nbody.cuh); the stage's stream function would be
+    overwritten.  Per pair of the step: 14.5 credited flops against the FP32
+    FMA peak.  The XU pipe bounds the step: it delivers 16 MUFU results per
+    clock per SM (each reciprocal or log2 holds it two cycles: ncu shows the
+    final kernel's XU pipe 94.5 % busy at 47.9 % of its instruction peak when
+    every reciprocal is a MUFU one), so 16 pairs per clock per SM in the stage
+    and 16 / 1.625 in the final evaluation, 2 / (1/16 + 1.625/16) = 12.2 for
+    the step."""
     peak, sm_max, nsm = fp32_peak(device)
     ach = pairs_per_s * 14.5 / 1e12
-    xu_pairs = 2 / (1 / 16 + 1 / 8) * nsm * sm_max * 1e6
+    mufu_final = 2 - 3 / 8
+    xu_pairs = 2 / (1 / 16 + mufu_final / 16) * nsm * sm_max * 1e6
     return {"bound": "fp32", "achieved": round(ach, 2), "peak": round(peak, 2), "unit": "TFLOP/s",
             "frac": round(ach / peak, 4), "traffic": None,
             "kernel": "nbody_chord<float,2,u> + nbody_chord<float,2,u,psi>, whole RK2 step timed",

@@ -233,13 +233,15 @@ __device__ __forceinline__ void two_sum_acc(double& s, double& c, double p) {
 // log2), and a MUFU result holds the XU pipe two cycles (16 per clock per SM),
 // while the pair's 8 FP32 lane operations leave half of the FP32 pipe (128
 // lanes per clock per SM) idle.  The Newton reciprocal costs 6 FP32 lane
-// operations (3 packed FMAs) and one integer operation; with 4 sources in 8
-// both pipes bound the loop at ~10.7 pairs per clock per SM instead of 8.
+// operations (3 packed FMAs) and one integer operation.  Measured on the
+// planar RK2 step (quad level 9), against the MUFU for every source: 1
+// source in 8 +4.3 %, 2 in 8 +8 %, 3 in 8 +9.4 %, 4 in 8 +4.8 %, 6 in 8 -2 %
+// (the issue slots the Newton steps take count as well).
 // The choice depends on the source's index alone (tiles and chunks start at
 // multiples of 8), so a target's sums do not depend on the kernel shape or the
 // chunking.  The velocity-only kernels keep the MUFU for every source.
 __host__ __device__ constexpr unsigned soft_rcp_sources(int ndim, bool wu, bool wp) {
-  return (ndim == 2 && wu && wp) ? 0x55u : 0u;
+  return (ndim == 2 && wu && wp) ? 0x25u : 0u;
 }
 
 // -1/q for a packed pair of positive normal floats, by Newton's method on the
