@@ -49,3 +49,13 @@ def test_seed_and_newton_steps():
     ulp = np.spacing(exact.astype(np.float32)).astype(np.float64)
     assert (np.abs(r - exact) <= 0.5 * ulp + 1e-300).mean() > 0.999
     assert (np.abs(r - exact) <= ulp).all()
+
+
+def test_bench_bound_matches_the_kernel_pattern():
+    """bench.py's XU bound for the planar step counts the MUFU reciprocals the
+    final kernel keeps: the popcount of soft_rcp_sources' pattern (of 8)."""
+    body = SRC.read_text().split("constexpr unsigned soft_rcp_sources(", 1)[1].split("\n}", 1)[0]
+    pattern = int(re.search(r"\? 0x([0-9A-Fa-f]+)u : 0u", body).group(1), 16)
+    bench = (Path(__file__).resolve().parents[1] / "bench.py").read_text()
+    m = re.search(r"mufu_final = 2 - (\d) / 8", bench)
+    assert m and int(m.group(1)) == bin(pattern).count("1")
