@@ -214,6 +214,8 @@ def run_ours(args, rank, world, device):
     ctx = core.Context(device)
     stream = torch.cuda.current_stream(device)
     ctx.set_stream(stream)
+    if args.fp32_shape is not None:  # else the stepper times the shapes once
+        ctx.set_kernel_shape(args.fp32_shape)
 
     host = make_state(args.level)
     vx, fx, fa, fm, vz, fz = host
@@ -1535,8 +1537,8 @@ def main():
     ap.add_argument("--ff-weights", default=None,
                     help="c5: load a saved network instead of training")
     ap.add_argument("--plane-level", type=int, default=9)
-    ap.add_argument("--fp32-shape", type=int, default=None, choices=range(4),
-                    help="c3: fixed FP32 kernel shape instead of the per-size autotuner")
+    ap.add_argument("--fp32-shape", type=int, default=None, choices=range(6),
+                    help="c2/c3: fixed FP32 kernel shape instead of the per-size autotuner")
     ap.add_argument("--problems", type=int, default=256)
     ap.add_argument("--ens-plan", default=None,
                     help="c4: fixed plan 'chunk_len,shape,persistent' instead of the autotuner")

@@ -87,11 +87,12 @@ int lpm_context_set_stream(lpm_context* ctx, void* cuda_stream);
 /* LPM_FP64 (default), LPM_FP64_EXACT, LPM_FP64_CHORD or LPM_FP32C for the
  * functor entry points below. */
 int lpm_context_set_precision(lpm_context* ctx, int precision);
-/* Fixes the FP32 N-body kernel shape (0-3: 256x4 with 3 or 4 CTAs per SM,
- * 128x8, 256x2, as for lpm_ensemble_set_kernel) of later LPM_FP32C functor
- * calls and of steppers created afterwards (a stepper keeps the shape it was
- * created with), or (-1, the default) lets each problem size time the four
- * shapes once and keep the fastest.  A target's sums do not depend on the
+/* Fixes the FP32 N-body kernel shape (0-5: 256x4 with 3 or 4 CTAs per SM,
+ * 128x8 with 4, 256x2 with 5, 128x8 with 3, 256x4 with 2; the same table as
+ * lpm_ensemble_set_kernel) of later LPM_FP32C functor calls and of steppers
+ * created afterwards (a stepper keeps the shape it was created with), or (-1,
+ * the default) lets each problem size time the six shapes once and keep the
+ * fastest.  A target's sums do not depend on the
  * shape. */
 int lpm_context_set_kernel_shape(lpm_context* ctx, int shape);
 /* Waits for the context's stream, then reports LPM_ERR_TIMEOUT if a bounded
@@ -327,8 +328,8 @@ int lpm_ensemble_nbody_time(lpm_ensemble* e, double* ms, int64_t* launches);
  * item, longest first; nullable). */
 int lpm_ensemble_shape(lpm_ensemble* e, int* threads, int* targets_per_thread,
                        int* persistent);
-/* Fixes the FP32 kernel shape (0-3: 256x4 with 3 or 4 CTAs per SM, 128x8,
- * 256x2) and the launch form (persistent 1 or one CTA per item 0); with
+/* Fixes the FP32 kernel shape (0-5, as for lpm_context_set_kernel_shape)
+ * and the launch form (persistent 1 or one CTA per item 0); with
  * lpm_ensemble_set_chunk_len, instead of autotuning.  Results do not depend
  * on either.  Call before the first velocity/step call. */
 int lpm_ensemble_set_kernel(lpm_ensemble* e, int shape, int persistent);

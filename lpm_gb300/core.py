@@ -247,7 +247,7 @@ class Context:
         self.precision = precision
 
     def set_kernel_shape(self, shape: int) -> None:
-        """Fixes the FP32 N-body kernel shape (0-3) of later LPM_FP32C sums,
+        """Fixes the FP32 N-body kernel shape (0-5) of later LPM_FP32C sums,
         or -1 for per-size autotuning (the default)."""
         check(lib().lpm_context_set_kernel_shape(self._h, int(shape)))
 

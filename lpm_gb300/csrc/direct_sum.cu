@@ -271,7 +271,10 @@ void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
     static_assert(kF32Shapes[0].nt == 256 && kF32Shapes[0].r == 4 && kF32Shapes[0].minb == 3 &&
                       kF32Shapes[1].nt == 256 && kF32Shapes[1].r == 4 && kF32Shapes[1].minb == 4 &&
                       kF32Shapes[2].nt == 128 && kF32Shapes[2].r == 8 && kF32Shapes[2].minb == 4 &&
-                      kF32Shapes[3].nt == 256 && kF32Shapes[3].r == 2 && kF32Shapes[3].minb == 5,
+                      kF32Shapes[3].nt == 256 && kF32Shapes[3].r == 2 && kF32Shapes[3].minb == 5 &&
+                      kF32Shapes[4].nt == 128 && kF32Shapes[4].r == 8 && kF32Shapes[4].minb == 3 &&
+                      kF32Shapes[5].nt == 256 && kF32Shapes[5].r == 4 && kF32Shapes[5].minb == 2 &&
+                      kNumF32Shapes == 6,
                   "launch table out of sync with kF32Shapes");
     switch (p.shape) {
       case 1:
@@ -282,6 +285,12 @@ void launch_chord_k(lpm_context& ctx, const NbodyPlan& p, const void* tgt,
         break;
       case 3:
         launch_chord_shape<T, NDIM, WU, WP, SKIPC, 2, 256, 5>(ctx, p, tgt, src, part, c0);
+        break;
+      case 4:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 8, 128, 3>(ctx, p, tgt, src, part, c0);
+        break;
+      case 5:
+        launch_chord_shape<T, NDIM, WU, WP, SKIPC, 4, 256, 2>(ctx, p, tgt, src, part, c0);
         break;
       default:
         launch_chord_shape<T, NDIM, WU, WP, SKIPC, 4, 256, 3>(ctx, p, tgt, src, part, c0);

@@ -292,12 +292,17 @@ struct lpm_ensemble {
       static_assert(lpm::kF32Shapes[0].nt == 256 && lpm::kF32Shapes[0].r == 4 &&
                         lpm::kF32Shapes[1].nt == 256 && lpm::kF32Shapes[1].r == 4 &&
                         lpm::kF32Shapes[2].nt == 128 && lpm::kF32Shapes[2].r == 8 &&
-                        lpm::kF32Shapes[3].nt == 256 && lpm::kF32Shapes[3].r == 2,
+                        lpm::kF32Shapes[3].nt == 256 && lpm::kF32Shapes[3].r == 2 &&
+                        lpm::kF32Shapes[4].nt == 128 && lpm::kF32Shapes[4].r == 8 &&
+                        lpm::kF32Shapes[5].nt == 256 && lpm::kF32Shapes[5].r == 4 &&
+                        lpm::kNumF32Shapes == 6,
                     "ensemble launch table out of sync with kF32Shapes");
       occupancy(0, lpm::ens_nbody<float, 4, 256, lpm::F32_TILE, 3>, 256);
       occupancy(1, lpm::ens_nbody<float, 4, 256, lpm::F32_TILE, 4>, 256);
       occupancy(2, lpm::ens_nbody<float, 8, 128, lpm::F32_TILE, 4>, 128);
       occupancy(3, lpm::ens_nbody<float, 2, 256, lpm::F32_TILE, 5>, 256);
+      occupancy(4, lpm::ens_nbody<float, 8, 128, lpm::F32_TILE, 3>, 128);
+      occupancy(5, lpm::ens_nbody<float, 4, 256, lpm::F32_TILE, 2>, 256);
     } else {
       occupancy(0, lpm::ens_nbody<double, lpm::F64_R, lpm::F64_NT, lpm::F64_TILE, 1>,
                 lpm::F64_NT);
@@ -410,6 +415,12 @@ struct lpm_ensemble {
           break;
         case 3:
           launch_f32<2, 256, 5>(grid);
+          break;
+        case 4:
+          launch_f32<8, 128, 3>(grid);
+          break;
+        case 5:
+          launch_f32<4, 256, 2>(grid);
           break;
         default:
           launch_f32<4, 256, 3>(grid);

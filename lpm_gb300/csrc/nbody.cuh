@@ -845,12 +845,14 @@ constexpr int F64_NT = 128, F64_R = 2, F64_TILE = 256;
 struct F32Shape {
   int nt, r, minb;
 };
-constexpr int kNumF32Shapes = 4;
+constexpr int kNumF32Shapes = 6;
 constexpr F32Shape kF32Shapes[kNumF32Shapes] = {
     {256, 4, 3},  // <= 85 registers: 24 warps / SM
     {256, 4, 4},  // <= 64 registers: 32 warps / SM
     {128, 8, 4},  // <= 128 registers: 16 warps, 8 targets per source load
     {256, 2, 5},  // <= 51 registers: 40 warps / SM
+    {128, 8, 3},  // <= 170 registers: 12 warps, 8 targets per source load
+    {256, 4, 2},  // <= 128 registers: 16 warps / SM
 };
 
 }  // namespace lpm

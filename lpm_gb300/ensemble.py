@@ -90,7 +90,7 @@ class BVEEnsemble:
         return a.value, b.value, bool(c.value)
 
     def set_kernel(self, shape: int, persistent: bool):
-        """Fixes the kernel shape (index 0-3) and launch form (before the
+        """Fixes the kernel shape (index 0-5) and launch form (before the
         first evaluation, together with set_chunk_len)."""
         check(lib().lpm_ensemble_set_kernel(self._h, int(shape), int(bool(persistent))))
 

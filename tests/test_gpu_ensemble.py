@@ -83,7 +83,7 @@ def test_ensemble_kernel_forms_agree(gpu_ctx):
     levels = [3, 1, 4, 2]
     params = [random_vortex_params(rng) for _ in levels]
     outs = []
-    for shape in range(4):
+    for shape in range(6):
         for persistent in (True, False):
             ens = BVEEnsemble(levels, params, 0.005, eps=0.01, flags=core.STEP_SKIP_MASKED_TARGETS,
                               ctx=ctx)

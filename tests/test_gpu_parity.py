@@ -233,7 +233,7 @@ def test_fp32_kernel_shapes_agree(gpu_ctx, oracle, geom, eps):
     dvx, dfx, dz, da, dm = dev(vx), dev(fx), dev(zf), dev(fa), dev(fm)
     outs = []
     try:
-        for shape in range(4):
+        for shape in range(6):
             ctx.set_kernel_shape(shape)
             u = torch.zeros(vx.shape[0], nd, dtype=torch.float64, device="cuda")
             p = torch.zeros(vx.shape[0], dtype=torch.float64, device="cuda")
@@ -252,7 +252,7 @@ def test_fp32_kernel_shapes_agree(gpu_ctx, oracle, geom, eps):
     assert rel(outs[0][0].cpu(), u_p) < TOL32
     assert rel(outs[0][1].cpu(), psi_p) < TOL32
     with pytest.raises(core.LpmError):
-        ctx.set_kernel_shape(4)
+        ctx.set_kernel_shape(6)
 
 
 def test_argument_errors(gpu_ctx):
