@@ -548,9 +548,9 @@ constexpr int kSph32NC = 27;  // A3 B3 U1[3] V1[3] U2[6] V2[6] Z G H
 
 struct __align__(16) SphPair32 {
   float4 hxy;  // x hi of sources 2k, 2k + 1; y hi of 2k, 2k + 1
-  float4 hzr;  // z hi; rot / (2 pi)
+  float4 hzr;  // z hi; rot / pi (twice rs: see above)
   float4 lxy;  // x lo (x - x hi); y lo
-  float4 lzp;  // z lo; pot / (2 pi)
+  float4 lzp;  // z lo; pot / pi
 };
 
 __global__ void k_swe_sphere32_pack(View fx, const double* __restrict__ zeta,
