@@ -619,6 +619,11 @@ def run_c5_leg(args, ctx, stream, device, weights):
                                  {"theta": r["theta"], "rho_min": r["rho_min"],
                                   "value": r["value"], "linf": r["error_vs_fp64"]["linf"]})
                              for f, r in best.items()},
+            # the learned correction moves the frontier only if its fastest
+            # setting at <= 1e-4 beats the expansion's fastest there
+            "learned_faster_than_expansion_at_1e-4": (
+                None if best["learned"] is None or best["expansion_only"] is None
+                else best["learned"]["value"] > best["expansion_only"]["value"]),
             "steps_timed_per_setting": args.c5_steps,
             "interactions_per_step": 4 * ipe}
 
