@@ -8,7 +8,8 @@
 //
 // The epilogue's SiLU (one tanh.approx.f32 per activation) keeps the
 // special-function unit busier than the tensor core: it, not the MMA, bounds
-// the inference kernel (packed BF16 tanh measured no faster on this part).
+// the inference kernel (packed BF16 or f16 tanh, one MUFU instruction per two
+// activations, measured no faster on this part).
 //
 // Tile = 128 rows (one target block against one cell at inference, 128
 // training samples in training) x one layer: tcgen05.mma with M = 128,
