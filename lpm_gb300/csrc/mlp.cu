@@ -7,9 +7,10 @@
 // 128 -> 16, SiLU, BF16 weights and activations, FP32 accumulation in TMEM.
 //
 // The epilogue's SiLU (one tanh.approx.f32 per activation) keeps the
-// special-function unit busier than the tensor core: it, not the MMA, bounds
-// the inference kernel (packed BF16 or f16 tanh, one MUFU instruction per two
-// activations, measured no faster on this part).
+// special-function unit busier than the tensor core (about 62 % of its cycles
+// against 25 %); with the TMEM loads, barriers and MMA waits between the four
+// warpgroups it bounds the inference kernel, not the MMA.  Packed BF16 or f16
+// tanh (one MUFU instruction per two activations) measured no faster.
 //
 // Tile = 128 rows (one target block against one cell at inference, 128
 // training samples in training) x one layer: tcgen05.mma with M = 128,
