@@ -1,6 +1,6 @@
-"""Ensemble stepper: each problem advanced inside the ensemble (one
-persistent launch per evaluation for all problems) matches the same problem
-advanced alone by BVERK4 in the same arithmetic."""
+"""Ensemble stepper: each problem advanced inside the ensemble (one N-body
+launch per evaluation for all problems, persistent or one CTA per work item)
+matches the same problem advanced alone by BVERK4 in the same arithmetic."""
 import math
 
 import numpy as np
@@ -96,3 +96,37 @@ def test_ensemble_kernel_forms_agree(gpu_ctx):
             ens.close()
     for o in outs[1:]:
         assert torch.equal(outs[0][0], o[0]) and torch.equal(outs[0][1], o[1])
+
+
+def test_ensemble_c4_scale(gpu_ctx):
+    """64 problems drawn like the C4 workload (levels 3-6, 1-4 Gaussian
+    vortices each), the plan autotuned over chunk length, the six kernel
+    shapes and both launch forms (thousands of work items): one evaluation
+    agrees with each sampled problem evaluated alone, FP32C against FP32C
+    (different chunkings: 2e-6)."""
+    ctx = gpu_ctx
+    rng = np.random.default_rng(20261204)
+    levels = [int(v) for v in rng.integers(3, 7, size=64)]
+    params = [random_vortex_params(rng) for _ in levels]
+    eps = 0.01
+    flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
+    ens = BVEEnsemble(levels, params, 0.005, eps=eps, precision=core.FP32C, flags=flags, ctx=ctx)
+    ens.velocity()
+    ctx.synchronize()
+    info = ens.info()
+    assert info["items"] > 1000 and info["chunk_len"] % 512 == 0
+    picks = [int(np.argmax(levels)), int(np.argmin(levels)), 31]
+    for p in picks:
+        sph = BVESphere(levels[p], ctx=ctx)
+        sph.init_vorticity(core.IC_MULTI_GAUSSIAN, params[p])
+        ctx.set_precision(core.FP32C)
+        F.ic2d_passive_sums(ctx, sph.velocity_verts, None, sph.vert_x, sph.face_x,
+                            sph.rel_vort_faces, sph.face_area, sph.face_mask, eps)
+        F.ic2d_active_sums(ctx, sph.velocity_faces, None, sph.face_x, sph.rel_vort_faces,
+                           sph.face_area, sph.face_mask, eps, self_rule=1)
+        ctx.synchronize()
+        vs, fs = ens.problem_slices(p)
+        leaf = sph.host_face_mask == 0
+        assert rel(ens.vvel[vs].cpu(), sph.velocity_verts.cpu()) < 2e-6, p
+        assert rel(ens.fvel[fs].cpu().numpy()[leaf], sph.velocity_faces.cpu().numpy()[leaf]) < 2e-6, p
+    ens.close()
