@@ -288,6 +288,10 @@ def run_ours(args, rank, world, device):
             flush.fill_(1.0)
             advance(h2, st2)
         core.check(core.lib().lpm_bve_rk4_nbody_time(h2, C.byref(msn), C.byref(nn)))
+        shp = [C.c_int() for _ in range(3)]
+        core.check(core.lib().lpm_bve_rk4_kernel_shape(h2, *[C.byref(v) for v in shp]))
+        kernel_shape = "%d threads x %d targets, %d CTAs per SM (autotuned)" % tuple(
+            v.value for v in shp)
         core.lib().lpm_bve_rk4_destroy(h2)
         nbody_ms = msn.value / max(nn.value, 1)
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
@@ -390,7 +394,9 @@ def run_ours(args, rank, world, device):
                          "frac": round(achieved / peak_fp32, 4), "traffic": traffic,
                          "peak_kind": f"computed FP32 FMA peak 2*128*{nsm} SMs*{sm_max:.0f} MHz "
                                       "(sm_max_mhz of MEASURED_PEAKS.json)",
-                         "kernel": "nbody_f32<3,u> (sphere velocity, FP32 pairs, compensated)",
+                         "kernel": "nbody_chord<float,3,u> (sphere velocity, FP32 pairs, "
+                                   "compensated)",
+                         "kernel_shape": kernel_shape,
                          "kernel_ms": round(nbody_ms, 4),
                          "flops_per_pair_credited": FLOPS_PER_PAIR,
                          "measured_fma_tflops": {"fp32": round(fma32, 2), "fp64": round(fma64, 3)},

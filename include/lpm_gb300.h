@@ -231,6 +231,12 @@ int lpm_bve_rk4_advance_timestep(lpm_bve_rk4* st, lpm_view vx, double* vzeta,
 /* With LPM_STEP_TIME_NBODY: total device time (ms) and number of the N-body
  * launches since the previous call (then reset).  Synchronous. */
 int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches);
+/* The N-body kernel shape the stepper runs: threads per CTA, targets per
+ * thread and the CTAs per SM its register cap is set for (LPM_FP32C: the
+ * autotuned one of the six shapes; FP64 forms: the fixed shape, 0 CTAs).
+ * Valid after the first step (LPM_ERR_STATE before). */
+int lpm_bve_rk4_kernel_shape(lpm_bve_rk4* st, int* threads, int* targets_per_thread,
+                             int* min_ctas_per_sm);
 
 typedef struct lpm_ic2d_rk2 lpm_ic2d_rk2;
 /* Incompressible2DRK2(dt, ic2d) (src/lpm_incompressible2d_rk2_impl.hpp:15-43).

@@ -157,6 +157,13 @@ class BVERK4:
         check(lib().lpm_bve_rk4_nbody_time(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def kernel_shape(self) -> tuple[int, int, int]:
+        """(threads per CTA, targets per thread, CTAs per SM of the register
+        cap) of the N-body kernel this stepper runs; after the first step."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().lpm_bve_rk4_kernel_shape(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def close(self) -> None:
         if self._h:
             lib().lpm_bve_rk4_destroy(self._h)

@@ -68,7 +68,7 @@ EXPORTS = [
     "lpm_mesh_face_vertices", "lpm_vtk_write_polymesh", "lpm_bve_direct_sum",
     "lpm_plane_direct_sum", "lpm_bve_rk4_step", "lpm_ic2d_rk2_step", "lpm_ensemble_run",
     "lpm_one_call_release", "lpm_wait_selftest", "lpm_ensemble_shape", "lpm_ensemble_set_kernel",
-    "lpm_netcdf_write_polymesh", "lpm_context_set_kernel_shape",
+    "lpm_netcdf_write_polymesh", "lpm_context_set_kernel_shape", "lpm_bve_rk4_kernel_shape",
 ]
 
 
@@ -143,6 +143,7 @@ def _declare(L: C.CDLL) -> None:
         "lpm_ic_eval": [i32, vp, i32, i32, i64, vp, vp],
         "lpm_measure_fma_peak": [vp, i32, C.POINTER(dbl)],
         "lpm_bve_rk4_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
+        "lpm_bve_rk4_kernel_shape": [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)],
         "lpm_ic2d_rk2_nbody_time": [vp, C.POINTER(dbl), C.POINTER(i64)],
         "lpm_bve_vertex_velocity_static": [V, V, i64, V, vp, vp, vp, i64, vp],
         "lpm_ensemble_create": [vp, C.POINTER(C.c_void_p), i32, vp, vp, vp, dbl, dbl, dbl, i32,

@@ -519,6 +519,25 @@ int lpm_bve_rk4_nbody_time(lpm_bve_rk4* st, double* ms, int64_t* launches) {
   }
 }
 
+int lpm_bve_rk4_kernel_shape(lpm_bve_rk4* st, int* threads, int* targets_per_thread,
+                             int* min_ctas_per_sm) {
+  if (!st || !threads || !targets_per_thread || !min_ctas_per_sm)
+    return lpm::fail(LPM_ERR_ARG, "null argument");
+  if (!st->ready)
+    return lpm::fail(LPM_ERR_STATE, "lpm_bve_rk4_kernel_shape: no step taken yet");
+  if (st->precision == LPM_FP32C) {
+    const lpm::F32Shape& k = lpm::kF32Shapes[st->plan.shape];
+    *threads = k.nt;
+    *targets_per_thread = k.r;
+    *min_ctas_per_sm = k.minb;
+  } else {
+    *threads = lpm::F64_NT;
+    *targets_per_thread = lpm::F64_R;
+    *min_ctas_per_sm = 0;
+  }
+  return LPM_OK;
+}
+
 int lpm_ic2d_rk2_nbody_time(lpm_ic2d_rk2* st, double* ms, int64_t* launches) {
   try {
     if (!st || !ms || !launches) return lpm::fail(LPM_ERR_ARG, "null argument");

@@ -131,6 +131,31 @@ def test_graph_replay_equals_direct(gpu_ctx):
         assert torch.equal(out[0][0], o[0]) and torch.equal(out[0][1], o[1])
 
 
+def test_stepper_reports_its_kernel_shape(gpu_ctx):
+    """lpm_bve_rk4_kernel_shape: an error before the first step; afterwards
+    the shape fixed through lpm_context_set_kernel_shape (index 3: 256
+    threads x 2 targets, 5 CTAs per SM), or one of the six autotuned ones."""
+    ctx = gpu_ctx
+    table = {(256, 4, 3), (256, 4, 4), (128, 8, 4), (256, 2, 5), (128, 8, 3), (256, 4, 2)}
+    for fixed in (3, -1):
+        ctx.set_kernel_shape(fixed)
+        try:
+            sph = BVESphere(4, ctx=ctx)
+            sph.init_vorticity(core.IC_RH54, rossby_haurwitz_params())
+            ctx.set_precision(core.FP32C)
+            sph.init_velocity()
+            st = BVERK4(0.01, sph, precision=core.FP32C)
+            with pytest.raises(core.LpmError):
+                st.kernel_shape()
+            st.advance_timestep(sph)
+            ctx.synchronize()
+            shape = st.kernel_shape()
+            assert shape == (256, 2, 5) if fixed == 3 else shape in table
+            st.close()
+        finally:
+            ctx.set_kernel_shape(-1)
+
+
 @pytest.mark.parametrize("precision", [core.FP64, core.FP64_CHORD, core.FP32C])
 @pytest.mark.parametrize("case", ["sphere0", "sphere_eps", "plane"])
 def test_ic2d_rk2(gpu_ctx, oracle, precision, case):
