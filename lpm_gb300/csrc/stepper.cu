@@ -45,6 +45,7 @@ struct lpm_stepper_base {
   bool ready = false;
   int64_t nsrc = 0, nft = 0, T = 0;
   lpm::NbodyPlan plan{};
+  int shape_u = 0;  // FP32 shape of the velocity-only evaluation (RK2 stage)
   std::vector<void*> allocs;
   int *slot2src = nullptr, *src2slot = nullptr, *fslot = nullptr, *tself = nullptr;
   void *tgt = nullptr, *src = nullptr;
@@ -110,6 +111,13 @@ struct lpm_stepper_base {
     LPM_CUDA(cudaStreamSynchronize(c.stream));
     // kernel shape for this problem size (the zeroed tiles time like real ones)
     plan.shape = lpm::tune_shape(c, plan, tgt, tself, src, part, eps);
+    shape_u = plan.shape;
+    if (plan.wp) {  // the RK2 stage evaluation runs the velocity-only kernel
+      lpm::NbodyPlan pu = plan;
+      pu.wp = false;
+      pu.ncomp = plan.ncomp - 1;
+      shape_u = lpm::tune_shape(c, pu, tgt, tself, src, part, eps);
+    }
     LPM_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     ready = true;
   }
@@ -182,6 +190,7 @@ struct lpm_stepper_base {
     if (plan.wp && !wp) {
       pl.wp = false;
       pl.ncomp = plan.ncomp - 1;
+      pl.shape = shape_u;
     }
     if (ff) {
       cudaEvent_t e[2];
