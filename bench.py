@@ -528,8 +528,8 @@ def run_other_legs(args, device):
 
 
 C5_SETTINGS = (  # (form, theta, rho_min): the configuration's setting first
-    ("learned", 0.5, 0.25), ("learned", 0.45, 0.25), ("learned", 0.4, 0.30),
-    ("learned", 0.35, 0.30),
+    ("learned", 0.5, 0.25), ("learned", 0.5, 0.30), ("learned", 0.5, 0.35),
+    ("learned", 0.45, 0.25), ("learned", 0.4, 0.30), ("learned", 0.35, 0.30),
     ("expansion_only", 0.5, None), ("expansion_only", 0.4, None), ("expansion_only", 0.35, None),
     ("expansion_only", 0.3, None))
 NET_MODE = {"expansion_only": 0, "learned": 1}
