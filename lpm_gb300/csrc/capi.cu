@@ -222,7 +222,9 @@ int lpm_context_set_precision(lpm_context* ctx, int precision) {
 int lpm_context_set_kernel_shape(lpm_context* ctx, int shape) {
   if (!ctx) return fail(LPM_ERR_ARG, "null context");
   if (shape < -1 || shape >= lpm::kNumF32Shapes)
-    return fail(LPM_ERR_ARG, "lpm_context_set_kernel_shape: shape must be -1 or 0-3");
+    return fail(LPM_ERR_ARG, ("lpm_context_set_kernel_shape: shape must be -1 (autotune) or 0-" +
+                              std::to_string(lpm::kNumF32Shapes - 1))
+                                 .c_str());
   ctx->forced_shape = shape;
   return LPM_OK;
 }

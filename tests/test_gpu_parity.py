@@ -251,8 +251,9 @@ def test_fp32_kernel_shapes_agree(gpu_ctx, oracle, geom, eps):
         oracle.set_sphere_form(False)
     assert rel(outs[0][0].cpu(), u_p) < TOL32
     assert rel(outs[0][1].cpu(), psi_p) < TOL32
-    with pytest.raises(core.LpmError):
-        ctx.set_kernel_shape(6)
+    for bad in (6, -2):
+        with pytest.raises(core.LpmError, match="0-5"):
+            ctx.set_kernel_shape(bad)
 
 
 def test_argument_errors(gpu_ctx):
