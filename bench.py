@@ -1032,7 +1032,7 @@ def run_plane(args, device):
     ctx = core.Context(device)
     stream = torch.cuda.current_stream(device)
     ctx.set_stream(stream)
-    if args.fp32_shape is not None:  # else the stepper times the four shapes once
+    if args.fp32_shape is not None:  # else the stepper times the six shapes once
         ctx.set_kernel_shape(args.fp32_shape)
     ic = Incompressible2D(core.MESH_QUAD_RECT, args.plane_level, radius=4.0, eps=0.02, ctx=ctx)
     ic.init_vorticity(core.IC_DIPOLE_PAIR, colliding_dipoles_params())
