@@ -541,10 +541,12 @@ def run_c5_leg(args, ctx, stream, device, weights):
     eps = 0.01, RK4 dt = 0.005, the octree far field (leaves <= 64, order-4
     expansion, exact FP32C near field) with the network trained earlier in
     this run (its inputs are scale-free: trained on levels 5-8).  For each
-    setting of C5_SETTINGS: one evaluation of 16,384 seeded targets against
-    the GPU FP64 direct sum (reference arithmetic) and the mean of --c5-steps
-    timed RK4 steps after one warm-up step.  The FP64 time per evaluation is
-    the sample's scaled to all targets."""
+    setting of C5_SETTINGS: one evaluation of every target, its error against
+    the GPU FP64 direct sum (reference arithmetic) on 16,384 seeded targets
+    and against the FP32C direct sum on every target (the larger of the two
+    decides "<= 1e-4"), and the mean of --c5-steps timed RK4 steps after one
+    warm-up step.  The FP64 time per evaluation is the sample's scaled to all
+    targets."""
     import torch
 
     from lpm_gb300 import core
@@ -573,6 +575,13 @@ def run_c5_leg(args, ctx, stream, device, weights):
     torch.cuda.synchronize(device)
     fp64_ms = a.elapsed_time(b) * xall.shape[0] / xs.shape[0]
     fp64 = ipe / (fp64_ms * 1e-3) / 1e9
+    # every target: the FP32C direct sum (1.5e-7 from FP64, checked on the
+    # sample) as the reference, since the sample's maximum misses the peaks
+    ctx.set_precision(core.FP32C)
+    uall32 = torch.zeros_like(xall)
+    F.ic2d_passive_sums(ctx, uall32, None, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
+    torch.cuda.synchronize(device)
+    fp32c_vs_fp64 = rel_errors(uall32[idx], u64)
     flags = core.STEP_SKIP_MASKED_TARGETS | core.STEP_REPROJECT
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
     st = st0.clone()
@@ -586,6 +595,7 @@ def run_c5_leg(args, ctx, stream, device, weights):
         ff.velocity(uall, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
         torch.cuda.synchronize(device)
         err = rel_errors(uall[idx], u64)
+        err_all = rel_errors(uall, uall32)
         run = st.clone()
         h = make_stepper(ctx, run, core.FP64_CHORD, flags)
         core.check(core.lib().lpm_bve_rk4_set_farfield(h, ff.handle, 0))
@@ -604,17 +614,24 @@ def run_c5_leg(args, ctx, stream, device, weights):
         ms /= args.c5_steps
         rows.append({"form": form, "theta": theta, "rho_min": rho,
                      "value": round(4 * ipe / (ms * 1e-3) / 1e9, 1), "ms_per_step": round(ms, 2),
-                     "error_vs_fp64": err, "network_rows": ff.stats().get("network_rows")
+                     "error_vs_fp64": err, "error_all_targets_vs_fp32c_direct": err_all,
+                     "network_rows": ff.stats().get("network_rows")
                      if form != "expansion_only" else 0})
         ff.close()
     spec = rows[0]
-    ok = [r for r in rows if r["error_vs_fp64"]["linf"] <= 1e-4]
+
+    def worst(r):
+        return max(r["error_vs_fp64"]["linf"], r["error_all_targets_vs_fp32c_direct"]["linf"])
+
+    ok = [r for r in rows if worst(r) <= 1e-4]
     best = {f: max((r for r in ok if r["form"] == f), key=lambda r: r["value"], default=None)
             for f in NET_MODE}
     return {"workload": "BVE sphere icosahedral level 8 RK4, Rossby-Haurwitz R=4, eps=0.01, "
                         "dt=0.005, octree far field (leaves <= 64, order-4 expansion)",
             "value": spec["value"], "unit": UNIT, "theta": spec["theta"],
             "rho_min": spec["rho_min"], "error_vs_fp64": spec["error_vs_fp64"],
+            "error_all_targets_vs_fp32c_direct": spec["error_all_targets_vs_fp32c_direct"],
+            "fp32c_direct_vs_fp64_on_sample": fp32c_vs_fp64,
             "fp64_direct": {"value": round(fp64, 3), "unit": UNIT,
                             "ms_per_evaluation": round(fp64_ms, 1),
                             "note": "GPU FP64 direct sum (reference kernel), 16,384 seeded "
@@ -623,7 +640,7 @@ def run_c5_leg(args, ctx, stream, device, weights):
             "settings": rows,
             "best_at_1e-4": {f: (None if r is None else
                                  {"theta": r["theta"], "rho_min": r["rho_min"],
-                                  "value": r["value"], "linf": r["error_vs_fp64"]["linf"]})
+                                  "value": r["value"], "linf": worst(r)})
                              for f, r in best.items()},
             # the learned correction moves the frontier only if its fastest
             # setting at <= 1e-4 beats the expansion's fastest there
@@ -1397,13 +1414,18 @@ def run_c5(args, device):
     b.record(stream)
     torch.cuda.synchronize(device)
     fp64_eval_s = a.elapsed_time(b) * 1e-3 * xall.shape[0] / xs.shape[0]
+    ctx.set_precision(core.FP32C)  # every target: the FP32C direct sum as the reference
+    uall32 = torch.zeros_like(xall)
+    F.ic2d_passive_sums(ctx, uall32, None, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
     uall = torch.zeros_like(xall)
-    errs = {}
+    errs, errs_all = {}, {}
     for tag, net in (("expansion_only", False), ("learned", True)):
         ff.set_network(net)
         ff.velocity(uall, xall, st0.fx, st0.fz, st0.fa, st0.fm, EPS)
         torch.cuda.synchronize(device)
         errs[tag] = rel_errors(uall[idx], u64)
+        errs_all[tag] = rel_errors(uall, uall32)
+    errs_all["fp32c_direct_vs_fp64_on_the_16384_targets"] = rel_errors(uall32[idx], u64)
     stats = ff.stats()
     ff.set_network(True)
     # ---- RK4 steps on the learned far field --------------------------------
@@ -1507,6 +1529,7 @@ def run_c5(args, device):
                             "note": "reference arithmetic on 16,384 seeded targets, scaled "
                                     "linearly to all targets"},
             "errors_one_evaluation_vs_fp64_direct_16384_targets": errs,
+            "errors_one_evaluation_all_targets_vs_fp32c_direct": errs_all,
             "errors_after_steps_vs_fp32c_direct": traj,
             "far_field": {**stats, "tree_ms_per_evaluation": round(tree_ms / max(nev, 1), 3),
                           "network_ms_per_evaluation": round(net_ms / max(nev, 1), 3)},
