@@ -12,8 +12,13 @@ namespace lpm {
 
 constexpr int kMaxLeaf = 64;        // largest leaf the kernels stage
 constexpr int kTargetBlock = 128;   // targets per block = rows of one MMA tile
-constexpr int kFarCap = 1024;       // far cells per target block
-constexpr int kNearCap = 640;       // near leaves per target block
+// List capacities per target block (28 KB of lists per 128 targets).  A block
+// whose lists overflow is summed directly; at icosahedral level 8 these hold
+// every block's lists down to theta = 0.2 (with 640 near leaves, 2 blocks
+// overflowed at theta = 0.26 and 30 at 0.2, and their direct sums doubled the
+// evaluation time).
+constexpr int kFarCap = 2048;       // far cells per target block
+constexpr int kNearCap = 4096;      // near leaves per target block
 constexpr int kLearnCap = 1024;     // learned (cell, block) pairs per block
 constexpr int kExactMax = 32;       // accepted cells with fewer points are summed exactly
 
