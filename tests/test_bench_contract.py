@@ -37,3 +37,29 @@ def test_bench_arguments_parse():
     assert r.returncode == 0
     for flag in ("--config", "--ff-theta", "--ff-rho-min", "--swe-level", "--no-learned"):
         assert flag in r.stdout
+
+
+def _bench_module():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("lpm_bench", ROOT / "bench.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_far_field_settings_are_valid():
+    """The level-8 leg's settings: the configuration's own (learned, theta
+    0.5) first, every form known, every rho_min inside [0, theta] (the far
+    field rejects a larger one, and the expansion-only rows use 0.25), and at
+    least one setting of each form."""
+    b = _bench_module()
+    form, theta, rho = b.C5_SETTINGS[0]
+    assert (form, theta) == ("learned", 0.5)
+    for form, theta, rho in b.C5_SETTINGS:
+        assert form in b.NET_MODE
+        assert 0.0 < theta <= 1.0
+        used = rho if rho else 0.25
+        assert 0.0 <= used <= theta, (form, theta, rho)
+        assert (rho is None) == (form == "expansion_only")
+    assert {f for f, _, _ in b.C5_SETTINGS} == set(b.NET_MODE)
